@@ -1,0 +1,290 @@
+"""Benchmark: FP64 cell-updates/s of the explicit finite-volume step on 1 GB300.
+
+Workload (single large unstructured mesh): Delaunay triangulation of a
+708 x 708 seeded jittered lattice on the unit square (about 1.0M triangles),
+Morton-ordered; bed = 8 Gaussian bumps (heights U[0.05,0.3], widths
+U[0.02,0.1]) over a flat floor at 0; surface 0.5 for x < 0.3 else 0.2, raised
+to the bed where bumps emerge; HLLC + Einfeldt; SSPRK2; dt = CFLdt() with the
+reference's coefficient 0.15 before every step.  A "step" is one full SSPRK2
+step (2 stages: reconstruction, fluxes with the CFL reduction, update) of the
+whole mesh.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Prints one JSON line.  value = cells x steps / device time of K steps replayed
+from a CUDA graph with the state resident in HBM; e2e = the same through the
+C ABI with host buffers (swe_set_prim + swe_step + swe_get_prim per step, the
+copies inside the timed region).  --impl reference times the CPU restatement
+of the reference solver on the host cores instead.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+# Compulsory HBM bytes of one ideally fused SSPRK2 cell-step (FP64 state, int32
+# connectivity): per stage read prim 24 + write prim 24 + 6 ids 24 + node xyz
+# 24 x N/C ~ 12 = 84 B; stage 2 re-reads the step's initial state, 24 B.
+BYTES_PER_CELL_STEP = 2 * 84 + 24
+LATTICE = int(os.environ.get("SWE_BENCH_LATTICE", "708"))
+CFL = 0.15
+
+
+def workload():
+    from swe_fvm_gb300 import scenarios
+
+    t0 = time.time()
+    mesh, prim = scenarios.dam_break(lattice=LATTICE)
+    return mesh, prim, time.time() - t0
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) == 7:
+                self.rows.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({n for r in self.rows for n, v in zip(names, r[3:]) if v.strip().lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def cpu_baseline(mesh, prim, budget_s: float = 10.0):
+    """The single-threaded CPU restatement on a bounded sample of the same workload."""
+    from oracle.oracle import Oracle
+
+    o = Oracle(mesh, prim)
+    o.compute_interface_values()
+    o.compute_fluxes()
+    t0 = time.perf_counter()
+    o.step("SSPRK2", CFL * o.min_len_to_wavespeed())
+    t1 = time.perf_counter() - t0
+    n_more = max(0, min(30, int(budget_s / max(t1, 1e-9)) - 1))
+    t0 = time.perf_counter()
+    for _ in range(n_more):
+        o.step("SSPRK2", CFL * o.min_len_to_wavespeed())
+    t = t1 + (time.perf_counter() - t0)
+    n = 1 + n_more
+    return {"value": mesh.num_cells * n / t, "unit": "cell-updates/s", "cores": 1, "kind": "port",
+            "sample": f"{n} SSPRK2 steps of the full {mesh.num_cells}-cell mesh, single thread, {t:.1f} s"}
+
+
+def dist_setup(n_gpus):
+    import torch
+
+    if n_gpus > 1 or "WORLD_SIZE" in os.environ:
+        import torch.distributed as dist
+
+        local = int(os.environ.get("LOCAL_RANK", "0"))
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+        return dist, dist.get_rank(), dist.get_world_size(), local
+    return None, 0, 1, 0
+
+
+def run_gpu(args):
+    import torch
+
+    from swe_fvm_gb300 import Fluxes, SpaceDisc, TimeDisc, Wavespeeds, _lib
+
+    dist, rank, world, local = dist_setup(args.gpus)
+    torch.cuda.set_device(local)
+    mesh, prim, t_gen = workload()
+    C = mesh.num_cells
+    sd = SpaceDisc(Fluxes.HLLC(Wavespeeds.Einfeldt), mesh, prim, cfl=CFL)
+    stream = torch.cuda.current_stream()
+    sd.set_stream(stream.cuda_stream)
+    # warm-up (graph capture happens on the first replay)
+    sd.run_cfl(1, args.warmup)
+    torch.cuda.synchronize()
+    n0 = sd.launch_count()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        _lib.check(_lib.load().swe_run_cfl(sd.ctx, 1, args.steps, None), sd.ctx)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    launches = sd.launch_count() - n0
+    if dist:
+        t = torch.tensor([ms], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        dist.barrier()
+    sd.synchronize()
+    value = world * C * args.steps / (ms * 1e-3)
+    ms_step = ms / args.steps
+
+    # per-kernel CUDA-event timings (kernel by kernel, same stream)
+    kt = sd.time_kernels(1, 3)
+    names = ["recon_pass1", "recon_pass2", "flux", "draining_dt", "update"]
+    per = {n: float(v) for n, v in zip(names, kt[:5])}
+
+    # end to end through the C ABI with host buffers
+    pinned = torch.empty((C, 3), dtype=torch.float64, pin_memory=True)
+    host = pinned.numpy()
+    host[:] = sd.GetVolField()
+    L = _lib.load()
+    dt = TimeDisc(sd).CFLdt()
+    n_e2e = max(3, min(args.steps, 20))
+    for _ in range(2):
+        L.swe_set_prim(sd.ctx, host.ctypes.data)
+        L.swe_step(sd.ctx, 1, dt)
+        L.swe_get_prim(sd.ctx, host.ctypes.data)
+    t0 = time.perf_counter()
+    for _ in range(n_e2e):
+        _lib.check(L.swe_set_prim(sd.ctx, host.ctypes.data), sd.ctx)
+        _lib.check(L.swe_step(sd.ctx, 1, dt), sd.ctx)
+        _lib.check(L.swe_get_prim(sd.ctx, host.ctypes.data), sd.ctx)
+    e2e_s = time.perf_counter() - t0
+    e2e = {"value": world * C * n_e2e / e2e_s, "unit": "cell-updates/s", "h2d_bytes_per_step": 24 * C,
+           "d2h_bytes_per_step": 24 * C, "steps": n_e2e,
+           "api": "swe_set_prim + swe_step + swe_get_prim (pinned host buffers)"}
+
+    hbm, src = peaks()
+    achieved = BYTES_PER_CELL_STEP * C / (ms_step * 1e-3) / 1e9
+    roof = {"bound": "hbm", "kernel": "ssprk2_step (2 stages x 5 kernels, one CUDA graph)", "achieved": achieved,
+            "peak": hbm, "unit": "GB/s", "frac": achieved / hbm, "peak_source": src,
+            "algorithmic_bytes_per_launch": BYTES_PER_CELL_STEP * C,
+            "traffic": TRAFFIC_PER_STEP.get(LATTICE),
+            "kernel_ms_per_launch": per}
+
+    out = {
+        "metric": "cell-updates/s (plain FP64 SSPRK2 step, 1M-triangle unstructured mesh)",
+        "value": value, "unit": "cell-updates/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded jittered-lattice Delaunay mesh, Gaussian bumps, dam break)",
+        "config": {"workload": "dam_break_1M", "cells": C, "edges": mesh.num_edges, "nodes": mesh.num_nodes,
+                   "flux": "HLLC+Einfeldt", "scheme": "SSPRK2", "cfl": CFL, "dt": "CFLdt() per step, on device",
+                   "l2": "working set > 1 GB, larger than the 129 MB L2; no flush",
+                   "parallelism": f"replicas x{world}", "mesh_gen_s": round(t_gen, 1)},
+        "e2e": e2e, "gpu_launches": launches, "roofline": roof, "clocks": clk.summary(),
+    }
+    if rank == 0:
+        if world == 1 and not args.no_cpu:
+            out["cpu_baseline"] = cpu_baseline(mesh, prim)
+        print(json.dumps(out), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+# DRAM bytes per SSPRK2 step from the ncu launch capture (sum over the step's
+# 10 kernels); filled from the committed profile summary.
+TRAFFIC_PER_STEP = {}
+
+
+def run_reference(args):
+    """CPU restatement of the reference solver (the reference cannot be built
+    here: Eigen is fetched from the network at configure time)."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from oracle.oracle import Oracle
+
+    mesh, prim, _ = workload()
+    C = mesh.num_cells
+    o = Oracle(mesh, prim)
+    o.compute_interface_values()
+    o.compute_fluxes()
+    for _ in range(min(args.warmup, 1)):
+        o.step("SSPRK2", CFL * o.min_len_to_wavespeed())
+    budget = 120.0
+    done, t = 0, 0.0
+    while done < args.steps:
+        t0 = time.perf_counter()
+        o.step("SSPRK2", CFL * o.min_len_to_wavespeed())
+        t += time.perf_counter() - t0
+        done += 1
+        if t > budget:
+            break
+    value = C * done / t
+    sample = f"{done} of {args.steps} SSPRK2 steps of the full {C}-cell mesh, single thread ({t:.1f} s)"
+    out = {"impl": "reference", "metric": "cell-updates/s (plain FP64 SSPRK2 step, 1M-triangle unstructured mesh)",
+           "value": value, "unit": "cell-updates/s", "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
+           "steps": done, "warmup": args.warmup, "ms_per_step": 1e3 * t / done, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": {"workload": "dam_break_1M", "cells": C, "flux": "HLLC+Einfeldt", "scheme": "SSPRK2",
+                      "cfl": CFL},
+           "cpu_baseline": {"value": value, "unit": "cell-updates/s", "cores": 1, "kind": "port", "sample": sample},
+           "e2e": {"value": value, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,186 @@
+/*
+ * swe_fvm_gb300.h -- C ABI of the GB300 explicit finite-volume shallow-water
+ * step (FP64, unstructured triangles, wet/dry MUSCL + HLL/HLLC + SSP-RK).
+ *
+ * One `swe_ctx` is the device-resident counterpart of the reference's
+ * SpaceDisc + TimeDisc pair (include/SpaceDisc.h:20-48, include/TimeDisc.h:4-23
+ * of NikitaMatckevich/SWE_FVM); `swe_step` is one call of
+ * Solvers::Euler / SSPRK2 / SSPRK3 (include/Solvers.h:6-8).  A `swe_batch`
+ * holds many independent instances stepped together.
+ *
+ * Conventions
+ *   - Arrays are the reference's layouts, host memory unless a name ends in
+ *     `_device`.  Geometry: 3 x N column-major doubles (node i's x, y, z at
+ *     [3i, 3i+1, 3i+2]; z is the bathymetry).  Topology: int64 row-major
+ *     edge_nodes E x 2, edge_cells E x 2 (owner, neighbour or -1 = solid wall),
+ *     cell_nodes / cell_edges / cell_neighbours C x 3.  Primitive state: 3 x C
+ *     column-major (w, u, v) per cell, w = free-surface level.
+ *   - The library copies every input; callers may free them after the call
+ *     (the reference keeps references: include/TriangMesh.h:56-64).
+ *   - Every function returns a swe_status; on failure the message is in
+ *     swe_last_error(ctx) (or swe_last_error(NULL) for a failed create).
+ *   - A context is not thread-safe (the reference is single-threaded);
+ *     distinct contexts may run concurrently on distinct streams.
+ *   - All state lives on the current CUDA device at create time.
+ */
+#ifndef SWE_FVM_GB300_H
+#define SWE_FVM_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Error classes.  Replaces the reference's exceptions DomainError / SolverError
+ * (include/Exceptions.h:4-10) and std::runtime_error (include/Assigners.h:20). */
+typedef enum swe_status {
+  SWE_OK = 0,
+  SWE_ERR_INVALID_ARGUMENT = 1,
+  SWE_ERR_INVALID_MESH = 2, /* bad index, non-manifold edge, boundary code other than -1 */
+  SWE_ERR_NONFINITE = 3,    /* non-finite state detected on the device */
+  SWE_ERR_TIMEOUT = 4,      /* a bounded device wait gave up */
+  SWE_ERR_CUDA = 5,
+  SWE_ERR_OUT_OF_MEMORY = 6,
+  SWE_ERR_UNSUPPORTED = 7
+} swe_status;
+
+/* Flux plugin: Fluxes::HLL<W> / Fluxes::HLLC<W> (include/Fluxes.h:14-111). */
+typedef enum swe_flux { SWE_FLUX_HLL = 0, SWE_FLUX_HLLC = 1 } swe_flux;
+/* Wave-speed plugin: Wavespeeds::Rusanov / Davis / Einfeldt (src/Fluxes.cpp:5-26). */
+typedef enum swe_wavespeed { SWE_WS_RUSANOV = 0, SWE_WS_DAVIS = 1, SWE_WS_EINFELDT = 2 } swe_wavespeed;
+/* Time scheme: Solvers::Euler / SSPRK2 / SSPRK3 (src/Solvers.cpp:5-59). */
+typedef enum swe_scheme { SWE_SCHEME_EULER = 0, SWE_SCHEME_SSPRK2 = 1, SWE_SCHEME_SSPRK3 = 2 } swe_scheme;
+
+/* Mesh in the reference's arrays (Topology + Domain geometry). */
+typedef struct swe_mesh {
+  int64_t num_nodes;
+  int64_t num_edges;
+  int64_t num_cells;
+  const double* geometry;         /* 3 x num_nodes, column-major */
+  const int64_t* edge_nodes;      /* num_edges x 2 */
+  const int64_t* edge_cells;      /* num_edges x 2 */
+  const int64_t* cell_nodes;      /* num_cells x 3 */
+  const int64_t* cell_edges;      /* num_cells x 3 */
+  const int64_t* cell_neighbours; /* num_cells x 3 */
+} swe_mesh;
+
+/* Physical and numerical parameters.  Defaults (swe_params_default) are the
+ * reference's: HLLC + Einfeldt, cor = tau = 0 (SpaceDisc ctor,
+ * include/SpaceDisc.h:24), CFL coefficient 0.15 (include/TimeDisc.h:22). */
+typedef struct swe_params {
+  int32_t flux;      /* swe_flux */
+  int32_t wavespeed; /* swe_wavespeed */
+  double cor;        /* Coriolis parameter (SpaceDisc::m_cor) */
+  double tau;        /* friction (stored, unused by the reference: src/TimeDisc.cpp:38-39) */
+  double cfl;        /* TimeDisc::CFLdt() = cfl * min length-to-wavespeed ratio */
+  int32_t reorder;   /* 0: keep the caller's cell order, 1: Morton order internally */
+  int32_t block;     /* threads per block for the cell/edge kernels; 0 = tuned default */
+} swe_params;
+
+typedef struct swe_ctx swe_ctx;
+typedef struct swe_batch swe_batch;
+
+/* Fills *p with the reference defaults. */
+swe_status swe_params_default(swe_params* p);
+
+/* Builds a context: validates and copies the mesh, precomputes the static
+ * geometry on the host, uploads it and the initial primitive state (3 x C).
+ * Replaces Topology(...) + Domain(...) + SpaceDisc(fluxer, domain, v0, cor, tau)
+ * + TimeDisc(&sd) (include/TriangMesh.h:27-40, src/Bathymetry.cpp:6-8,
+ * src/SpaceDisc.cpp:4-13, include/TimeDisc.h:6-7). */
+swe_status swe_create(const swe_mesh* mesh, const double* prim0, const swe_params* params, swe_ctx** out);
+swe_status swe_destroy(swe_ctx* ctx);
+
+/* Runs kernels of this context on `stream` (a cudaStream_t; NULL = the
+ * context's own stream). */
+swe_status swe_set_stream(swe_ctx* ctx, void* stream);
+
+/* One time step of the scheme with a fixed dt: Solvers::X(&td, dt)
+ * (src/Solvers.cpp:5-59).  Asynchronous on the context's stream. */
+swe_status swe_step(swe_ctx* ctx, int32_t scheme, double dt);
+
+/* n_steps fixed-dt steps, replayed from a captured CUDA graph. */
+swe_status swe_run(swe_ctx* ctx, int32_t scheme, double dt, int64_t n_steps);
+
+/* n_steps steps with dt = TimeDisc::CFLdt() taken before every step from the
+ * previous flux pass (include/TimeDisc.h:13), all on the device.  If
+ * t_elapsed is not NULL it receives the sum of the dts (synchronises). */
+swe_status swe_run_cfl(swe_ctx* ctx, int32_t scheme, int64_t n_steps, double* t_elapsed);
+
+/* TimeDisc::CFLdt() (include/TimeDisc.h:13); synchronises. */
+swe_status swe_cfl_dt(swe_ctx* ctx, double* dt);
+/* SpaceDisc::GetMinLenToWavespeed() of the last flux pass (include/SpaceDisc.h:31). */
+swe_status swe_min_len_to_wavespeed(swe_ctx* ctx, double* r);
+
+/* SpaceDisc::ComputeInterfaceValues() / ComputeFluxes() (src/SpaceDisc.cpp:33-74)
+ * on the current state, for inspection with the getters below. */
+swe_status swe_compute_interface_values(swe_ctx* ctx);
+swe_status swe_compute_fluxes(swe_ctx* ctx);
+
+/* Primitive state, 3 x C column-major in the caller's cell order
+ * (VolumeField, include/ValueField.h:31-48).  Synchronous.  Setting the state
+ * leaves the CFL ratio of the last flux pass in place, as assigning the
+ * reference's volume field does. */
+swe_status swe_get_prim(swe_ctx* ctx, double* prim_out);
+swe_status swe_set_prim(swe_ctx* ctx, const double* prim_in);
+/* Same, from / to device memory in the caller's order, asynchronous on the
+ * context's stream. */
+swe_status swe_get_prim_device(swe_ctx* ctx, double* prim_out_device);
+swe_status swe_set_prim_device(swe_ctx* ctx, const double* prim_in_device);
+
+/* Interface values and source gradients in the reference's EdgeField layout:
+ * 3 x 2E column-major, slot 2e + (from < to) (include/ValueField.h:70-75);
+ * row 0 of `src` is unused by the reference and returned as 0.  Either pointer
+ * may be NULL.  Synchronous. */
+swe_status swe_get_edge_values(swe_ctx* ctx, double* edg_out, double* src_out);
+/* Edge fluxes, 3 x E (SpaceDisc::GetFluxes, include/SpaceDisc.h:28). */
+swe_status swe_get_fluxes(swe_ctx* ctx, double* flux_out);
+/* Node maxima of the reconstructed level after pass 1 of the last
+ * reconstruction (MUSCLObject::m_max_wp, include/MUSCLObject.h:68), N values. */
+swe_status swe_get_node_max(swe_ctx* ctx, double* max_out);
+
+/* Profiling: runs `reps` steps of `scheme` (CFL dt) launching the stage
+ * kernels one by one with CUDA events between them on the context's stream.
+ * out_ms[0..4] = mean duration of one launch of the reconstruction pass 1,
+ * pass 2, flux, draining-time-step and update kernels; out_ms[5] = mean step
+ * time.  Advances the state; synchronises.  No reference counterpart. */
+swe_status swe_time_kernels(swe_ctx* ctx, int32_t scheme, int64_t reps, double* out_ms);
+
+/* Size and counters. */
+swe_status swe_num_cells(swe_ctx* ctx, int64_t* n);
+/* Kernel launches issued so far by this context (all streams, graphs counted
+ * per kernel node replayed). */
+swe_status swe_launch_count(swe_ctx* ctx, int64_t* n);
+/* Blocks until the context's stream is idle and checks the device error word. */
+swe_status swe_synchronize(swe_ctx* ctx);
+
+/* Message of the last failure on ctx (NULL ctx: the last failure of a create
+ * on this thread).  Never NULL. */
+const char* swe_last_error(swe_ctx* ctx);
+
+/* ---------------------------------------------------------------- batched */
+/* Many independent instances (each its own mesh, state, parameters and CFL
+ * step) stepped together: cells and edges of all instances are concatenated
+ * and every stage kernel covers them all in one launch.  params may be one
+ * struct (n_params = 1) or one per instance. */
+swe_status swe_batch_create(int32_t n_instances, const swe_mesh* meshes, const double* const* prim0,
+                            const swe_params* params, int32_t n_params, swe_batch** out);
+swe_status swe_batch_destroy(swe_batch* b);
+/* n_steps steps of every instance, each with its own dt = cfl * ratio taken
+ * before every step; one CUDA graph per step replayed n_steps times. */
+swe_status swe_batch_run_cfl(swe_batch* b, int32_t scheme, int64_t n_steps);
+/* n_steps fixed-dt steps (same dt for every instance). */
+swe_status swe_batch_run(swe_batch* b, int32_t scheme, double dt, int64_t n_steps);
+swe_status swe_batch_get_prim(swe_batch* b, int32_t instance, double* prim_out);
+/* Sum of the dts taken by an instance so far. */
+swe_status swe_batch_time(swe_batch* b, int32_t instance, double* t);
+swe_status swe_batch_launch_count(swe_batch* b, int64_t* n);
+swe_status swe_batch_synchronize(swe_batch* b);
+const char* swe_batch_last_error(swe_batch* b);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SWE_FVM_GB300_H */

@@ -1,0 +1,862 @@
+/*
+ * swe_oracle.c -- CPU restatement of the SWE_FVM explicit finite-volume step.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file is the checker for the GPU library and
+ * the timed CPU baseline ("port" kind).  Only tests/, __graft_entry__.smoke()
+ * and bench.py's CPU legs may load it.  The product path never calls it.
+ *
+ * It restates, function by function, the reference solver (NikitaMatckevich/
+ * SWE_FVM, C++17 + Eigen) in plain C99 without Eigen.  Every function cites the
+ * reference file:line it follows.  It keeps the reference's structure on
+ * purpose (geometry recomputed on each call, neighbour classification redone
+ * inside loops, draining time step evaluated 4x per cell) because it doubles as
+ * the single-threaded CPU baseline.
+ *
+ * Documented deviations from the reference as written:
+ *   - Domain::E(e) (src/Bathymetry.cpp:29-31) returns an uninitialised point in
+ *     the reference.  Here it is the midpoint of the edge's two nodes (x,y,z).
+ *   - The unqualified abs() of include/Fluxes.h:45,88, src/Fluxes.cpp:8 and
+ *     src/PointOperations.cpp:13,32 is read as the floating-point fabs().
+ *   - ReconstructFullWetCell's positivity test (src/MUSCLObject.cpp:67-72)
+ *     subtracts the node bathymetry row b.P(ip).row(2) from the vertex values.
+ *   - order switch: ORACLE_ORDER_LITERAL reproduces the in-place sequential
+ *     semantics of src/Solvers.cpp:11-13,23-25,30-32 and src/SpaceDisc.cpp:47-51
+ *     (results depend on cell order); ORACLE_ORDER_JACOBI makes every read of a
+ *     stage come from the start-of-stage state and pass 2 of the reconstruction
+ *     read the pass-1 node maxima only.  JACOBI is the GPU parity target.
+ *   - Eigen 3.4's 2x2 partialPivLu solve is restated with the same pivot rule.
+ *
+ * Build: -O2 -ffp-contract=off (no FMA contraction, so results do not depend on
+ * whether the host compiler fuses multiply-adds).
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define ORACLE_ORDER_JACOBI 0
+#define ORACLE_ORDER_LITERAL 1
+
+#define FLUX_HLL 0
+#define FLUX_HLLC 1
+#define WS_RUSANOV 0
+#define WS_DAVIS 1
+#define WS_EINFELDT 2
+
+/* include/Includes.h:30 */
+static const double TOL = 1e-13;
+/* include/Bathymetry.h:5-8 */
+static int is_wet(double h) { return h > 1e-12; }
+
+/* std::min / std::max semantics: min(a,b) = (b < a) ? b : a; max(a,b) = (a < b) ? b : a */
+static double smin(double a, double b) { return (b < a) ? b : a; }
+static double smax(double a, double b) { return (a < b) ? b : a; }
+
+typedef struct {
+  int64_t num_nodes, num_edges, num_cells;
+  const double* geom;       /* 3 x N column-major (x,y,z per node) */
+  const int64_t* edge_nodes; /* E x 2 */
+  const int64_t* edge_cells; /* E x 2 */
+  const int64_t* cell_nodes; /* C x 3 */
+  const int64_t* cell_edges; /* C x 3 */
+  const int64_t* cell_nbrs;  /* C x 3 */
+} oracle_mesh;
+
+typedef struct {
+  double w0, u0, v0;  /* at_origin */
+  double g[3][2];     /* gradient, 3 x 2 */
+  int64_t i;
+} muscl_t;
+
+typedef struct oracle_ctx {
+  oracle_mesh m;
+  /* owned copies of the mesh arrays */
+  double* geom;
+  int64_t *en, *ec, *cn, *ce, *ct;
+  int flux, ws, order;
+  double cor, tau;
+  double* vol;      /* 3 x C prim (w,u,v) */
+  double* vol_snap; /* start-of-stage snapshot (jacobi reads) */
+  double* edg;      /* 3 x 2E prim */
+  double* src;      /* 3 x 2E (rows 1,2 used) */
+  double* f;        /* 3 x E */
+  double* max_wp;   /* N */
+  double* max_wp1;  /* N: pass-1 maxima (jacobi) */
+  double r;         /* m_min_length_to_wavespeed */
+  const double* vol_read; /* field read by classification / draining */
+  const double* maxwp_read;
+} oracle_ctx;
+
+/* ------------------------------------------------------------------ geometry */
+/* src/Bathymetry.cpp:20-22 */
+static const double* P(const oracle_ctx* c, int64_t n) { return c->geom + 3 * n; }
+
+/* src/PointOperations.cpp:4-6 */
+static double len2d(const double* a, const double* b) {
+  return sqrt((a[0] - b[0]) * (a[0] - b[0]) + (a[1] - b[1]) * (a[1] - b[1]));
+}
+/* src/PointOperations.cpp:8-10 */
+static double det2(const double* a, const double* b) { return a[0] * b[1] - b[0] * a[1]; }
+
+/* src/Bathymetry.cpp:24-27: (P(tp) * (1/3,1/3,1/3)) row by row */
+static void T(const oracle_ctx* c, int64_t t, double out[3]) {
+  const int64_t* tp = c->cn + 3 * t;
+  const double k = 1. / 3.;
+  for (int r = 0; r < 3; ++r)
+    out[r] = P(c, tp[0])[r] * k + P(c, tp[1])[r] * k + P(c, tp[2])[r] * k;
+}
+/* Edge centre: midpoint (deviation for the stub at src/Bathymetry.cpp:29-31) */
+static void E(const oracle_ctx* c, int64_t e, double out[3]) {
+  const double* a = P(c, c->en[2 * e]);
+  const double* b = P(c, c->en[2 * e + 1]);
+  for (int r = 0; r < 3; ++r) out[r] = (a[r] + b[r]) * 0.5;
+}
+/* src/Bathymetry.cpp:82-85 */
+static double L(const oracle_ctx* c, int64_t e) {
+  return len2d(P(c, c->en[2 * e]), P(c, c->en[2 * e + 1]));
+}
+/* src/Bathymetry.cpp:87-90, src/PointOperations.cpp:12-14 */
+static double Area(const oracle_ctx* c, int64_t t) {
+  const int64_t* tp = c->cn + 3 * t;
+  const double *a = P(c, tp[0]), *b = P(c, tp[1]), *cc = P(c, tp[2]);
+  double ba[2] = {b[0] - a[0], b[1] - a[1]};
+  double ca[2] = {cc[0] - a[0], cc[1] - a[1]};
+  return 0.5 * fabs(det2(ba, ca));
+}
+/* src/Bathymetry.cpp:69-76 */
+static void Tang(const oracle_ctx* c, int64_t e, int64_t t, double out[2]) {
+  const double* p0 = P(c, c->en[2 * e]);
+  const double* p1 = P(c, c->en[2 * e + 1]);
+  double l = L(c, e);
+  double tan[3] = {(p1[0] - p0[0]) / l, (p1[1] - p0[1]) / l, (p1[2] - p0[2]) / l};
+  double tt[3];
+  T(c, t, tt);
+  double d[3] = {tt[0] - p0[0], tt[1] - p0[1], tt[2] - p0[2]};
+  if (det2(d, tan) > 0.) {
+    tan[0] = -tan[0];
+    tan[1] = -tan[1];
+  }
+  out[0] = tan[0];
+  out[1] = tan[1];
+}
+/* src/Bathymetry.cpp:78-80: [[0,1],[-1,0]] * tang */
+static void Norm(const oracle_ctx* c, int64_t e, int64_t t, double out[2]) {
+  double tg[2];
+  Tang(c, e, t, tg);
+  out[0] = tg[1];
+  out[1] = -tg[0];
+}
+
+/* src/PointOperations.cpp:42-48: plane slope through three points (columns),
+ * 2x2 partial-pivot LU solve (Eigen's pivot rule: first row of largest |a_i0|). */
+static void Gradient3(const double p0[3], const double p1[3], const double p2[3], double g[2]) {
+  double a00 = p1[0] - p0[0], a01 = p1[1] - p0[1], b0 = p1[2] - p0[2];
+  double a10 = p2[0] - p0[0], a11 = p2[1] - p0[1], b1 = p2[2] - p0[2];
+  if (fabs(a10) > fabs(a00)) {
+    double t;
+    t = a00; a00 = a10; a10 = t;
+    t = a01; a01 = a11; a11 = t;
+    t = b0; b0 = b1; b1 = t;
+  }
+  double l10 = a10;
+  if (a00 != 0.) l10 = a10 / a00;
+  double u11 = a11 - l10 * a01;
+  double y1 = b1 - l10 * b0;
+  double x1 = y1 / u11;
+  double x0 = (b0 - a01 * x1) / a00;
+  g[0] = x0;
+  g[1] = x1;
+}
+/* src/Bathymetry.cpp:10-13 */
+static void TriangSlope(const oracle_ctx* c, int64_t t, double g[2]) {
+  const int64_t* tp = c->cn + 3 * t;
+  Gradient3(P(c, tp[0]), P(c, tp[1]), P(c, tp[2]), g);
+}
+
+/* src/TriangMesh.cpp:5-7, 18-23 */
+static int IsEdgeBoundary(const oracle_ctx* c, int64_t e) { return c->ec[2 * e + 1] < 0; }
+static int IsTriangleBoundary(const oracle_ctx* c, int64_t t) {
+  const int64_t* ie = c->ce + 3 * t;
+  return IsEdgeBoundary(c, ie[0]) || IsEdgeBoundary(c, ie[1]) || IsEdgeBoundary(c, ie[2]);
+}
+
+/* ----------------------------------------------------------- value fields */
+/* src/ValueField.cpp:8-10: volume bathymetry = centroid z */
+static double vol_b(const oracle_ctx* c, int64_t t) {
+  double tt[3];
+  T(c, t, tt);
+  return tt[2];
+}
+/* src/ValueField.cpp:13-15: edge bathymetry = E(e).z */
+static double edg_b(const oracle_ctx* c, int64_t e) {
+  double ee[3];
+  E(c, e, ee);
+  return ee[2];
+}
+/* include/ValueField.h:70-75 */
+static int64_t edge_id(int64_t e, int64_t from, int64_t to) { return 2 * e + (int64_t)(from < to); }
+
+static double vol_w(const oracle_ctx* c, const double* vol, int64_t i) { (void)c; return vol[3 * i]; }
+static double vol_h(const oracle_ctx* c, const double* vol, int64_t i) { return vol[3 * i] - vol_b(c, i); }
+
+/* src/Assigners.cpp:8-20: PrimAssigner::operator= into column col of a 3-row field */
+static void prim_assign(double* field, int64_t col, double b, const double rhs[3]) {
+  double h = rhs[0] - b;
+  double* d = field + 3 * col;
+  if (!is_wet(h)) {
+    d[0] = b; d[1] = 0.; d[2] = 0.;
+    return;
+  }
+  d[0] = rhs[0]; d[1] = rhs[1]; d[2] = rhs[2];
+  if (h < 1e-3) {
+    double s = 1.4142135623730951 * h / sqrt(h * h + 1e-6);
+    d[1] *= s;
+    d[2] *= s;
+  }
+}
+/* src/Assigners.cpp:28-44: ConsAssigner::operator= */
+static void cons_assign(double* field, int64_t col, double b, const double rhs[3]) {
+  double h = rhs[0];
+  double* d = field + 3 * col;
+  if (!is_wet(h)) {
+    d[0] = b; d[1] = 0.; d[2] = 0.;
+    return;
+  }
+  double ih;
+  if (h < 1e-3) ih = 1.4142135623730951 * h / sqrt(h * h * h * h + 1e-12);
+  else ih = 1. / h;
+  d[0] = h + b;
+  d[1] = rhs[1] * ih;
+  d[2] = rhs[2] * ih;
+}
+/* include/ValueField.h:34,39-41: cons = (h, h*u, h*v) */
+static void vol_cons(const oracle_ctx* c, const double* vol, int64_t i, double out[3]) {
+  double h = vol[3 * i] - vol_b(c, i);
+  out[0] = h;
+  out[1] = h * vol[3 * i + 1];
+  out[2] = h * vol[3 * i + 2];
+}
+
+/* ------------------------------------------------------------- MUSCL object */
+/* include/MUSCLObject.h:26-33 */
+static void muscl_at_point(const oracle_ctx* c, const muscl_t* m, const double p[3], double out[3]) {
+  double tt[3];
+  T(c, m->i, tt);
+  double d0 = p[0] - tt[0], d1 = p[1] - tt[1];
+  double a0 = m->w0 + (m->g[0][0] * d0 + m->g[0][1] * d1);
+  double a1 = m->u0 + (m->g[1][0] * d0 + m->g[1][1] * d1);
+  double a2 = m->v0 + (m->g[2][0] * d0 + m->g[2][1] * d1);
+  if ((a0 - p[2]) >= 0) {
+    out[0] = a0; out[1] = a1; out[2] = a2;
+  } else {
+    out[0] = p[2]; out[1] = 0.; out[2] = 0.;
+  }
+}
+/* include/MUSCLObject.h:35-48: gradient row 0 at point p */
+static void muscl_gradient_row0(const oracle_ctx* c, const muscl_t* m, const double p[3], double g[2]) {
+  double ap[3];
+  muscl_at_point(c, m, p, ap);
+  double h = ap[0] - p[2];
+  if (h >= 0) {
+    g[0] = m->g[0][0];
+    g[1] = m->g[0][1];
+  } else {
+    TriangSlope(c, m->i, g);
+  }
+}
+
+/* src/MUSCLObject.cpp:13-29 (classification reads the field c->vol_read) */
+static int IsDryCell(const oracle_ctx* c, int64_t i) { return !is_wet(vol_h(c, c->vol_read, i)); }
+static int IsFullWetCell(const oracle_ctx* c, int64_t i) {
+  if (IsTriangleBoundary(c, i)) return 0;
+  const int64_t* tp = c->cn + 3 * i;
+  double z0 = P(c, tp[0])[2], z1 = P(c, tp[1])[2], z2 = P(c, tp[2])[2];
+  double mx = z0;
+  if (z1 > mx) mx = z1;
+  if (z2 > mx) mx = z2;
+  return mx < vol_w(c, c->vol_read, i);
+}
+static int IsPartWetCell(const oracle_ctx* c, int64_t i) { return !IsDryCell(c, i) && !IsFullWetCell(c, i); }
+
+static void muscl_zero(muscl_t* m) { memset(m, 0, sizeof(*m)); }
+
+/* src/MUSCLObject.cpp:31-36 */
+static muscl_t ReconstructDryCell(const oracle_ctx* c, int64_t i) {
+  muscl_t m;
+  muscl_zero(&m);
+  double s[2];
+  TriangSlope(c, i, s);
+  m.g[0][0] = s[0];
+  m.g[0][1] = s[1];
+  m.w0 = vol_b(c, i);
+  m.u0 = 0.;
+  m.v0 = 0.;
+  m.i = i;
+  return m;
+}
+
+/* src/PointOperations.cpp:26-40 on the cubic of include/CubicPolyMath.h:13-15
+ * (coefficients in the reference's constructor order d, c, b). */
+static double cubic(double d, double cc, double b, double x) { return x * x * x + b * x * x + cc * x + d; }
+/* (int)log2(x) for finite x > 0 (truncation toward zero), taken exactly from
+ * the binary exponent so that it does not depend on the libm's log2 rounding. */
+static int trunc_log2(double x) {
+  int e;
+  double m = frexp(x, &e); /* x = m 2^e, m in [0.5, 1) */
+  if (m == 0.5) return e - 1;
+  return (e >= 1) ? e - 1 : e;
+}
+static double Bisection(double d, double cc, double b, double xmin, double xmax) {
+  double fmin_ = cubic(d, cc, b, xmin), fmax_ = cubic(d, cc, b, xmax);
+  if (signbit(fmin_) == signbit(fmax_)) return (fabs(fmin_) < fabs(fmax_)) ? xmin : xmax;
+  int n = 50 + trunc_log2(xmax - xmin);
+  double x = 0.;
+  for (int it = 0; it <= n; it++) {
+    x = 0.5 * (xmin + xmax);
+    if (signbit(cubic(d, cc, b, xmin)) != signbit(cubic(d, cc, b, x))) xmax = x;
+    else xmin = x;
+  }
+  return x;
+}
+
+/* src/MUSCLObject.cpp:86-112 */
+static muscl_t ReconstructPartWetCell1(const oracle_ctx* c, int64_t i) {
+  const int64_t* ip = c->cn + 3 * i;
+  double z0 = P(c, ip[0])[2], z1 = P(c, ip[1])[2], z2 = P(c, ip[2])[2];
+  double b13 = z0, b23 = z0;
+  if (z1 > b13) b13 = z1;
+  if (z2 > b13) b13 = z2;
+  if (z1 < b23) b23 = z1;
+  if (z2 < b23) b23 = z2;
+  double b12 = 3. * vol_b(c, i) - b23 - b13;
+  double b_delim = b12 + (1. / 3.) * (b13 - b12) * (b13 - b12) / (b13 - b23);
+  double w = vol_w(c, c->vol_read, i);
+  double h = vol_h(c, c->vol_read, i);
+  double w_rec;
+  if (w >= b13) {
+    w_rec = w;
+  } else if (w <= b_delim) {
+    w_rec = b23 + cbrt(3. * h * (b13 - b23) * (b12 - b23));
+  } else {
+    double a = -3. * b13;
+    double bb = 3. * (b12 * b13 + b13 * b23 - b12 * b23);
+    double cc = (b13 - b23) * (3. * h * (b13 - b12) - b12 * (b12 + b23)) - b23 * b23 * b13;
+    w_rec = Bisection(cc, bb, a, b12, b13);
+  }
+  muscl_t m;
+  muscl_zero(&m);
+  m.w0 = w_rec;
+  m.u0 = c->vol_read[3 * i + 1];
+  m.v0 = c->vol_read[3 * i + 2];
+  m.i = i;
+  return m;
+}
+
+/* src/MUSCLObject.cpp:38-84 */
+static muscl_t ReconstructFullWetCell(const oracle_ctx* c, int64_t i) {
+  const int64_t* ip = c->cn + 3 * i;
+  const int64_t* ie = c->ce + 3 * i;
+  const int64_t* it = c->ct + 3 * i;
+  const double* vol = c->vol_read;
+  double pts[3][3];
+  for (int k = 0; k < 3; ++k) {
+    if (IsFullWetCell(c, it[k])) {
+      T(c, it[k], pts[k]);
+    } else if (IsDryCell(c, it[k])) {
+      muscl_t m;
+      muscl_zero(&m);
+      m.w0 = vol[3 * i]; m.u0 = vol[3 * i + 1]; m.v0 = vol[3 * i + 2];
+      m.i = i;
+      return m;
+    } else {
+      /* the reference also evaluates ReconstructPartWetCell1(it[k]).AtPoint(E)
+       * into grad_values, which is never used (src/MUSCLObject.cpp:55-58) */
+      E(c, ie[k], pts[k]);
+    }
+  }
+  double df[3][2] = {{0, 0}, {0, 0}, {0, 0}};
+  Gradient3(pts[0], pts[1], pts[2], df[0]);
+
+  /* dx = (P(ip) * (I - 1/3)).topRows(2); column k, row r:
+   * P(r,0)*M(0,k) + P(r,1)*M(1,k) + P(r,2)*M(2,k) with M = I - 1/3 */
+  const double third = 1. / 3.;
+  const double diag = 1. - third;
+  double w = vol[3 * i];
+  int wet_all = 1;
+  for (int k = 0; k < 3; ++k) {
+    double dxk[2];
+    for (int r = 0; r < 2; ++r) {
+      double m0 = (k == 0) ? diag : -third;
+      double m1 = (k == 1) ? diag : -third;
+      double m2 = (k == 2) ? diag : -third;
+      dxk[r] = P(c, ip[0])[r] * m0 + P(c, ip[1])[r] * m1 + P(c, ip[2])[r] * m2;
+    }
+    double wp = (df[0][0] * dxk[0] + df[0][1] * dxk[1]) + w;
+    double hp = wp - P(c, ip[k])[2];
+    if (!is_wet(hp)) wet_all = 0;
+  }
+  if (!wet_all) {
+    df[0][0] = 0.; df[0][1] = 0.;
+  }
+
+  double tvd[3] = {1., 1., 1.};
+  double ti[3];
+  T(c, i, ti);
+  for (int k = 0; k < 3; ++k) {
+    double ek[3];
+    E(c, ie[k], ek);
+    double d0 = ek[0] - ti[0], d1 = ek[1] - ti[1];
+    for (int r = 0; r < 3; ++r) {
+      double a = vol[3 * i + r], b = vol[3 * it[k] + r];
+      double vmin = smin(a, b), vmax = smax(a, b);
+      double vek = a + (df[r][0] * d0 + df[r][1] * d1);
+      if (!((vmin <= vek) && (vek <= vmax))) tvd[r] = 0.;
+    }
+  }
+  muscl_t m;
+  m.w0 = vol[3 * i]; m.u0 = vol[3 * i + 1]; m.v0 = vol[3 * i + 2];
+  for (int r = 0; r < 3; ++r) {
+    m.g[r][0] = tvd[r] * df[r][0];
+    m.g[r][1] = tvd[r] * df[r][1];
+  }
+  m.i = i;
+  return m;
+}
+
+/* src/MUSCLObject.cpp:114-191 */
+static muscl_t ReconstructPartWetCell2(const oracle_ctx* c, int64_t i) {
+  int64_t ip[3] = {c->cn[3 * i], c->cn[3 * i + 1], c->cn[3 * i + 2]};
+  int64_t t;
+  if (P(c, ip[0])[2] > P(c, ip[1])[2]) { t = ip[0]; ip[0] = ip[1]; ip[1] = t; }
+  if (P(c, ip[1])[2] > P(c, ip[2])[2]) { t = ip[1]; ip[1] = ip[2]; ip[2] = t; }
+  if (P(c, ip[0])[2] > P(c, ip[1])[2]) { t = ip[0]; ip[0] = ip[1]; ip[1] = t; }
+  double b23 = P(c, ip[0])[2];
+  double b12 = P(c, ip[1])[2];
+  double b13 = P(c, ip[2])[2];
+  double w = vol_w(c, c->vol_read, i);
+  if ((w > b13) || (b13 - b23 < TOL)) return ReconstructPartWetCell1(c, i);
+
+  double w23 = c->maxwp_read[ip[0]];
+  double h23 = w23 - b23;
+  double ratio_b = (b12 - b23) / (b13 - b23);
+  double h_delim1 = 1. / 3. * h23 * ratio_b;
+  double h_delim2 = 1. / 3. * h23 * (2. * b13 - b12 - b23) / (b13 - b23);
+  double hi = vol_h(c, c->vol_read, i);
+  double ratio_h = hi / h23;
+
+  /* `points` is an Eigen Matrix3d whose COLUMNS are the three points (that is
+   * what Gradient() reads).  Eigen's points(r, c) is row r, column c, so the
+   * reference's points(0,2) / points(1,2) writes land in the x / y coordinate
+   * of point 2, which every branch then overwrites with points.col(2) = ...;
+   * only points(2,2) (the z of point 2) survives.  Point 0 therefore keeps the
+   * node bathymetry b23.  pts[k] below holds column k after all the writes. */
+  double pts[3][3];
+  const double *P0 = P(c, ip[0]), *P1 = P(c, ip[1]), *P2 = P(c, ip[2]);
+  for (int r = 0; r < 3; ++r) pts[0][r] = P0[r];
+
+  if (hi <= h_delim1) { /* one vertex wet */
+    double k2 = sqrt(3. * ratio_h / ratio_b);
+    for (int r = 0; r < 3; ++r) pts[1][r] = k2 * P1[r] + (1. - k2) * P0[r];
+    double k3 = sqrt(3. * ratio_h * ratio_b);
+    for (int r = 0; r < 3; ++r) pts[2][r] = k3 * P2[r] + (1. - k3) * P0[r];
+  } else if (hi >= h_delim2) { /* three vertices wet */
+    double delta_w = 1.5 * (hi - h_delim2);
+    for (int r = 0; r < 3; ++r) pts[1][r] = P1[r];
+    for (int r = 0; r < 3; ++r) pts[2][r] = P2[r];
+    pts[2][2] += delta_w;
+  } else { /* two vertices wet */
+    double alpha = 3. * ratio_h;
+    double beta = (b13 - b12) / (b13 - b23);
+    /* CubicPoly{d, c}: x^3 + c x + d, bisection on [0, 1] */
+    double k1 = 1. - Bisection((1. + beta - alpha) / (beta * beta), (alpha - 3.) / beta, 0., 0., 1.);
+    if (k1 < TOL) return ReconstructPartWetCell1(c, i);
+    double bp1 = k1 * b13 + (1. - k1) * b12;
+    for (int r = 0; r < 3; ++r) pts[1][r] = P1[r];
+    for (int r = 0; r < 3; ++r) pts[2][r] = k1 * P2[r] + (1. - k1) * P1[r];
+    pts[2][2] = bp1;
+  }
+  muscl_t m;
+  muscl_zero(&m);
+  Gradient3(pts[0], pts[1], pts[2], m.g[0]);
+  double ti[3];
+  T(c, i, ti);
+  double wt = w23 + (m.g[0][0] * (ti[0] - P0[0]) + m.g[0][1] * (ti[1] - P0[1]));
+  m.w0 = wt;
+  m.u0 = c->vol_read[3 * i + 1];
+  m.v0 = c->vol_read[3 * i + 2];
+  m.i = i;
+  return m;
+}
+
+/* ------------------------------------------------------------- SpaceDisc */
+/* src/SpaceDisc.cpp:15-31 */
+static void UpdateInterfaceValues(oracle_ctx* c, const muscl_t* m) {
+  int64_t i = m->i;
+  const int64_t* ip = c->cn + 3 * i;
+  const int64_t* ie = c->ce + 3 * i;
+  const int64_t* it = c->ct + 3 * i;
+  for (int k = 0; k < 3; ++k) {
+    double ap[3];
+    muscl_at_point(c, m, P(c, ip[k]), ap);
+    c->max_wp[ip[k]] = smax(c->max_wp[ip[k]], ap[0]);
+    double ec[3];
+    E(c, ie[k], ec);
+    double ae[3];
+    muscl_at_point(c, m, ec, ae);
+    int64_t id = edge_id(ie[k], i, it[k]);
+    prim_assign(c->edg, id, edg_b(c, ie[k]), ae);
+    double g[2];
+    muscl_gradient_row0(c, m, ec, g);
+    double u = c->edg[3 * id + 1], v = c->edg[3 * id + 2];
+    c->src[3 * id + 1] = g[0];
+    c->src[3 * id + 2] = g[1];
+    c->src[3 * id + 1] += c->cor * (-v);
+    c->src[3 * id + 2] += c->cor * u;
+  }
+}
+
+/* src/SpaceDisc.cpp:33-52 */
+void oracle_compute_interface_values(oracle_ctx* c) {
+  const int64_t N = c->m.num_nodes, C = c->m.num_cells;
+  for (int64_t n = 0; n < N; ++n) c->max_wp[n] = c->geom[3 * n + 2];
+  c->vol_read = c->vol;
+  for (int64_t i = 0; i < C; ++i) {
+    muscl_t m;
+    if (IsDryCell(c, i)) m = ReconstructDryCell(c, i);
+    else if (!IsFullWetCell(c, i)) m = ReconstructPartWetCell1(c, i);
+    else m = ReconstructFullWetCell(c, i);
+    UpdateInterfaceValues(c, &m);
+  }
+  if (c->order == ORACLE_ORDER_JACOBI) {
+    memcpy(c->max_wp1, c->max_wp, (size_t)N * sizeof(double));
+    c->maxwp_read = c->max_wp1;
+  } else {
+    c->maxwp_read = c->max_wp;
+  }
+  for (int64_t i = 0; i < C; ++i) {
+    if (IsPartWetCell(c, i)) {
+      muscl_t m = ReconstructPartWetCell2(c, i);
+      UpdateInterfaceValues(c, &m);
+    }
+  }
+}
+
+/* include/SpaceDisc.h:4-18 (g = 1) */
+static void ElemFlux(const double n[2], const double U[3], double out[3]) {
+  out[0] = 0.; out[1] = 0.; out[2] = 0.;
+  double h = U[0];
+  if (is_wet(h)) {
+    double hveln = U[1] * n[0] + U[2] * n[1];
+    out[0] = hveln;
+    out[1] = (hveln / h) * U[1] + (0.5 * h * h) * n[0];
+    out[2] = (hveln / h) * U[2] + (0.5 * h * h) * n[1];
+  }
+}
+
+/* src/Fluxes.cpp:5-26 */
+static void Wavespeed(int ws, double ul, double hl, double ur, double hr, double a[2]) {
+  double cl = sqrt(hl), cr = sqrt(hr);
+  if (ws == WS_RUSANOV) {
+    double ap = smax(fabs(ul) + cl, fabs(ur) + cr);
+    a[0] = -ap;
+    a[1] = ap;
+  } else if (ws == WS_DAVIS) {
+    a[0] = smin(ul - cl, ur - cr);
+    a[1] = smax(ul + cl, ur + cr);
+  } else {
+    double uRoe = (cl * ul + cl * ur) / (cl + cr);
+    double cRoe = sqrt(0.5 * (hl + hr));
+    a[0] = smin(ul - cl, uRoe - cRoe);
+    a[1] = smax(ur + cr, uRoe + cRoe);
+  }
+}
+
+static void edge_cons(const oracle_ctx* c, int64_t e, int64_t id, double U[3]) {
+  double h = c->edg[3 * id] - edg_b(c, e);
+  U[0] = h;
+  U[1] = h * c->edg[3 * id + 1];
+  U[2] = h * c->edg[3 * id + 2];
+}
+
+/* include/Fluxes.h:14-54 */
+static void FluxHLL(oracle_ctx* c, int64_t e, int64_t from, int64_t to, double* r, double out[3]) {
+  double n[2];
+  Norm(c, e, from, n);
+  int64_t il = edge_id(e, from, to), ir = edge_id(e, to, from);
+  double be = edg_b(c, e);
+  double ul = c->edg[3 * il + 1] * n[0] + c->edg[3 * il + 2] * n[1];
+  double hl = c->edg[3 * il] - be;
+  double ur = c->edg[3 * ir + 1] * n[0] + c->edg[3 * ir + 2] * n[1];
+  double hr = c->edg[3 * ir] - be;
+  out[0] = out[1] = out[2] = 0.;
+  if (hl + hr <= 1e-10) return;
+  double a[2];
+  Wavespeed(c->ws, ul, hl, ur, hr, a);
+  double al = smin(0., a[0]);
+  double ar = smax(0., a[1]);
+  if (ar - al <= 1e-10) return;
+  if (r) {
+    double dl = 2. * Area(c, from) / L(c, e);
+    double dr = 2. * Area(c, to) / L(c, e);
+    double cor = fabs(c->cor);
+    double lw = smin(dl, dr) / (cor + smax(-al, ar));
+    *r = smin(*r, lw);
+  }
+  double Ul[3], Ur[3], Fl[3], Fr[3];
+  edge_cons(c, e, il, Ul);
+  edge_cons(c, e, ir, Ur);
+  ElemFlux(n, Ul, Fl);
+  ElemFlux(n, Ur, Fr);
+  for (int q = 0; q < 3; ++q)
+    out[q] = (ar * Fl[q] - al * Fr[q] + (al * ar) * (Ur[q] - Ul[q])) / (ar - al);
+}
+
+/* include/Fluxes.h:56-111 */
+static void FluxHLLC(oracle_ctx* c, int64_t e, int64_t from, int64_t to, double* r, double out[3]) {
+  double t[2], n[2];
+  Tang(c, e, from, t);
+  Norm(c, e, from, n);
+  int64_t il = edge_id(e, from, to), ir = edge_id(e, to, from);
+  double be = edg_b(c, e);
+  double ul = c->edg[3 * il + 1] * n[0] + c->edg[3 * il + 2] * n[1];
+  double vl = c->edg[3 * il + 1] * t[0] + c->edg[3 * il + 2] * t[1];
+  double hl = c->edg[3 * il] - be;
+  double ur = c->edg[3 * ir + 1] * n[0] + c->edg[3 * ir + 2] * n[1];
+  double vr = c->edg[3 * ir + 1] * t[0] + c->edg[3 * ir + 2] * t[1];
+  double hr = c->edg[3 * ir] - be;
+  out[0] = out[1] = out[2] = 0.;
+  if (hl + hr <= 1e-10) return;
+  double a[2];
+  Wavespeed(c->ws, ul, hl, ur, hr, a);
+  double al = a[0], ar = a[1];
+  double ustar = (ar - ur) * hr * ur - (al - ul) * hl * ul + 0.5 * (hl * hl - hr * hr);
+  ustar /= (hr * (ar - ur) - hl * (al - ul));
+  if (r) {
+    double dl = 2. * Area(c, from) / L(c, e);
+    double dr = 2. * Area(c, to) / L(c, e);
+    double cor = fabs(c->cor);
+    double lw = smin(dl, dr) / (cor + smax(TOL, smax(al, ar)));
+    *r = smin(*r, lw);
+  }
+  double Ul[3], Ur[3], F[3];
+  edge_cons(c, e, il, Ul);
+  edge_cons(c, e, ir, Ur);
+  if (ustar <= 0) {
+    double us = vr * t[0] + ustar * t[1];
+    double vs = vr * n[0] + ustar * n[1];
+    double hs = hr * (ar - ur) / (ar - ustar);
+    double Us[3] = {hs, hs * us, hs * vs};
+    ElemFlux(n, Ur, F);
+    double s = smax(0., ar);
+    for (int q = 0; q < 3; ++q) out[q] = F[q] + s * (Us[q] - Ur[q]);
+  } else {
+    double us = vl * t[0] + ustar * t[1];
+    double vs = vl * n[0] + ustar * n[1];
+    double hs = hl * (al - ul) / (al - ustar);
+    double Us[3] = {hs, hs * us, hs * vs};
+    ElemFlux(n, Ul, F);
+    double s = smin(0., al);
+    for (int q = 0; q < 3; ++q) out[q] = F[q] + s * (Us[q] - Ul[q]);
+  }
+}
+
+/* src/SpaceDisc.cpp:54-74 */
+void oracle_compute_fluxes(oracle_ctx* c) {
+  c->r = 1.;
+  const int64_t E_ = c->m.num_edges;
+  for (int64_t e = 0; e < E_; ++e) {
+    int64_t lf = c->ec[2 * e], lt = c->ec[2 * e + 1];
+    double n[2];
+    Norm(c, e, lf, n);
+    double* fo = c->f + 3 * e;
+    if (lt == -1) {
+      double U[3] = {vol_h(c, c->vol, lf), 0., 0.};
+      ElemFlux(n, U, fo);
+    } else if (c->flux == FLUX_HLL) {
+      FluxHLL(c, e, lf, lt, &c->r, fo);
+    } else {
+      FluxHLLC(c, e, lf, lt, &c->r, fo);
+    }
+  }
+}
+
+/* ------------------------------------------------------------- TimeDisc */
+/* src/TimeDisc.cpp:43-66; reads the field c->vol_read */
+static double ComputeDrainingDt(const oracle_ctx* c, int64_t i) {
+  if (i < 0) return INFINITY;
+  if (IsDryCell(c, i)) return 0.;
+  const int64_t* ie = c->ce + 3 * i;
+  double sum = 0.;
+  for (int k = 0; k < 3; ++k) {
+    int64_t itk = c->ec[2 * ie[k]];
+    double f = c->f[3 * ie[k]];
+    sum += smax(0., (i == itk) ? f : -f);
+  }
+  return sum > TOL ? Area(c, i) * vol_h(c, c->vol_read, i) / sum : INFINITY;
+}
+
+/* src/TimeDisc.cpp:3-41 */
+static void RHS(const oracle_ctx* c, int64_t i, double dt, double res[3]) {
+  const int64_t* ie = c->ce + 3 * i;
+  const int64_t* it = c->ct + 3 * i;
+  res[0] = res[1] = res[2] = 0.;
+  double i_area = 1. / Area(c, i);
+  double dti = ComputeDrainingDt(c, i);
+  for (int k = 0; k < 3; ++k) {
+    int sgn = c->ec[2 * ie[k]] == i ? 1 : -1;
+    double dtik = ComputeDrainingDt(c, it[k]);
+    const double* fk = c->f + 3 * ie[k];
+    double dtk = (sgn * fk[0]) > 0. ? smin(dt, dti) : smin(dt, dtik);
+    double c_ek = i_area * L(c, ie[k]);
+    int64_t id = edge_id(ie[k], i, it[k]);
+    double h_ek = c->edg[3 * id] - edg_b(c, ie[k]);
+    double s = dtk * sgn * c_ek;
+    res[0] -= s * fk[0];
+    res[1] -= s * fk[1];
+    res[2] -= s * fk[2];
+    double q = dt * (1. / 3.);
+    res[1] -= q * c->src[3 * id + 1] * h_ek;
+    res[2] -= q * c->src[3 * id + 2] * h_ek;
+    double n[2];
+    Norm(c, ie[k], i, n);
+    double p = 0.5 * h_ek * h_ek;
+    res[1] += dtk * (n[0] * c_ek * p);
+    res[2] += dtk * (n[1] * c_ek * p);
+  }
+}
+
+/* ------------------------------------------------------------- Solvers */
+/* One Runge-Kutta stage in Shu-Osher form (src/Solvers.cpp:5-59):
+ *   stage 1:     vol(i) = U0.cons(i) + RHS(i, dt)
+ *   stage s > 1: vol(i) = a * U0.cons(i) + b * Uprev.cons(i) + RHS(i, c * dt)
+ * u0 is the step's initial state.  literal: writes in place while RHS reads the
+ * live field; jacobi: RHS reads the start-of-stage snapshot. */
+static void rk_stage(oracle_ctx* c, const double* u0, int first, double a, double b, double dt_stage) {
+  const int64_t C = c->m.num_cells;
+  oracle_compute_interface_values(c);
+  oracle_compute_fluxes(c);
+  if (c->order == ORACLE_ORDER_JACOBI) {
+    memcpy(c->vol_snap, c->vol, (size_t)C * 3 * sizeof(double));
+    c->vol_read = c->vol_snap;
+  } else {
+    c->vol_read = c->vol;
+  }
+  for (int64_t i = 0; i < C; ++i) {
+    double rhs[3], U0[3], nv[3];
+    RHS(c, i, dt_stage, rhs);
+    vol_cons(c, u0, i, U0);
+    if (first) {
+      nv[0] = U0[0] + rhs[0];
+      nv[1] = U0[1] + rhs[1];
+      nv[2] = U0[2] + rhs[2];
+    } else {
+      double U1[3];
+      /* the start-of-stage value of cell i (not yet overwritten in literal mode) */
+      vol_cons(c, c->vol, i, U1);
+      nv[0] = a * U0[0] + b * U1[0] + rhs[0];
+      nv[1] = a * U0[1] + b * U1[1] + rhs[1];
+      nv[2] = a * U0[2] + b * U1[2] + rhs[2];
+    }
+    cons_assign(c->vol, i, vol_b(c, i), nv);
+  }
+  c->vol_read = c->vol;
+}
+
+/* scheme: 0 Euler, 1 SSPRK2, 2 SSPRK3 (src/Solvers.cpp:5-14, 16-33, 35-59) */
+void oracle_step(oracle_ctx* c, int scheme, double dt) {
+  const int64_t C = c->m.num_cells;
+  double* u0 = (double*)malloc((size_t)C * 3 * sizeof(double));
+  memcpy(u0, c->vol, (size_t)C * 3 * sizeof(double));
+  rk_stage(c, u0, 1, 0., 0., dt);
+  if (scheme == 1) {
+    rk_stage(c, u0, 0, 0.5, 0.5, 0.5 * dt);
+  } else if (scheme == 2) {
+    rk_stage(c, u0, 0, 0.75, 0.25, 0.25 * dt);
+    rk_stage(c, u0, 0, 1. / 3., 2. / 3., 2. / 3. * dt);
+  }
+  free(u0);
+}
+
+/* include/TimeDisc.h:13,22 with the coefficient as a parameter */
+double oracle_min_len_to_wavespeed(const oracle_ctx* c) { return c->r; }
+
+static int64_t* dup_i64(const int64_t* p, int64_t n) {
+  int64_t* q = (int64_t*)malloc((size_t)(n > 0 ? n : 1) * sizeof(int64_t));
+  if (n > 0) memcpy(q, p, (size_t)n * sizeof(int64_t));
+  return q;
+}
+
+oracle_ctx* oracle_create(int64_t num_nodes, int64_t num_edges, int64_t num_cells, const double* geom,
+                          const int64_t* edge_nodes, const int64_t* edge_cells, const int64_t* cell_nodes,
+                          const int64_t* cell_edges, const int64_t* cell_nbrs, const double* prim0, int flux,
+                          int ws, double cor, double tau, int order) {
+  oracle_ctx* c = (oracle_ctx*)calloc(1, sizeof(oracle_ctx));
+  c->m.num_nodes = num_nodes;
+  c->m.num_edges = num_edges;
+  c->m.num_cells = num_cells;
+  c->geom = (double*)malloc((size_t)num_nodes * 3 * sizeof(double));
+  memcpy(c->geom, geom, (size_t)num_nodes * 3 * sizeof(double));
+  c->en = dup_i64(edge_nodes, 2 * num_edges);
+  c->ec = dup_i64(edge_cells, 2 * num_edges);
+  c->cn = dup_i64(cell_nodes, 3 * num_cells);
+  c->ce = dup_i64(cell_edges, 3 * num_cells);
+  c->ct = dup_i64(cell_nbrs, 3 * num_cells);
+  c->flux = flux;
+  c->ws = ws;
+  c->cor = cor;
+  c->tau = tau;
+  c->order = order;
+  c->vol = (double*)malloc((size_t)num_cells * 3 * sizeof(double));
+  c->vol_snap = (double*)malloc((size_t)num_cells * 3 * sizeof(double));
+  /* SpaceDisc copies v0 through the volume field (src/MUSCLObject.cpp:8-11) */
+  memcpy(c->vol, prim0, (size_t)num_cells * 3 * sizeof(double));
+  c->edg = (double*)calloc((size_t)num_edges * 6, sizeof(double));
+  c->src = (double*)calloc((size_t)num_edges * 6, sizeof(double));
+  c->f = (double*)calloc((size_t)num_edges * 3, sizeof(double));
+  c->max_wp = (double*)malloc((size_t)num_nodes * sizeof(double));
+  c->max_wp1 = (double*)malloc((size_t)num_nodes * sizeof(double));
+  c->vol_read = c->vol;
+  c->maxwp_read = c->max_wp;
+  c->r = 1.;
+  return c;
+}
+
+void oracle_destroy(oracle_ctx* c) {
+  if (!c) return;
+  free(c->geom); free(c->en); free(c->ec); free(c->cn); free(c->ce); free(c->ct);
+  free(c->vol); free(c->vol_snap); free(c->edg); free(c->src); free(c->f);
+  free(c->max_wp); free(c->max_wp1);
+  free(c);
+}
+
+void oracle_get_prim(const oracle_ctx* c, double* out) {
+  memcpy(out, c->vol, (size_t)c->m.num_cells * 3 * sizeof(double));
+}
+void oracle_set_prim(oracle_ctx* c, const double* in) {
+  memcpy(c->vol, in, (size_t)c->m.num_cells * 3 * sizeof(double));
+}
+/* edge fields in the reference layout: 3 x 2E each; fluxes 3 x E; node maxima N */
+void oracle_get_edge_fields(const oracle_ctx* c, double* edg, double* src, double* f, double* max_wp) {
+  if (edg) memcpy(edg, c->edg, (size_t)c->m.num_edges * 6 * sizeof(double));
+  if (src) memcpy(src, c->src, (size_t)c->m.num_edges * 6 * sizeof(double));
+  if (f) memcpy(f, c->f, (size_t)c->m.num_edges * 3 * sizeof(double));
+  if (max_wp) memcpy(max_wp, c->max_wp, (size_t)c->m.num_nodes * sizeof(double));
+}
+
+/* Per-cell class as the reconstruction pass 1 sees it: 0 dry, 1 part-wet, 2 full-wet */
+void oracle_classify(oracle_ctx* c, int32_t* out) {
+  c->vol_read = c->vol;
+  for (int64_t i = 0; i < c->m.num_cells; ++i)
+    out[i] = IsDryCell(c, i) ? 0 : (IsFullWetCell(c, i) ? 2 : 1);
+}
+
+/* Unit-level entry points for known-answer tests of the device functions. */
+void oracle_wavespeed(int ws, double ul, double hl, double ur, double hr, double* a) {
+  Wavespeed(ws, ul, hl, ur, hr, a);
+}
+double oracle_bisection_cubic(double d, double cc, double b, double xmin, double xmax) {
+  return Bisection(d, cc, b, xmin, xmax);
+}
+void oracle_gradient3(const double* p0, const double* p1, const double* p2, double* g) { Gradient3(p0, p1, p2, g); }
+void oracle_prim_assign(double b, const double* rhs, double* out) { prim_assign(out, 0, b, rhs); }
+void oracle_cons_assign(double b, const double* rhs, double* out) { cons_assign(out, 0, b, rhs); }

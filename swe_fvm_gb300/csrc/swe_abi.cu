@@ -1,0 +1,549 @@
+// swe_abi.cu -- the extern "C" boundary declared in include/swe_fvm_gb300.h.
+//
+// A swe_ctx is an Engine over one instance; a swe_batch is an Engine over many.
+// Every entry point validates its arguments, catches C++ exceptions and turns
+// CUDA errors into status codes with a message (the reference throws
+// DomainError / SolverError / std::runtime_error, include/Exceptions.h:4-10).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <exception>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/swe_fvm_gb300.h"
+#include "swe_engine.cuh"
+
+using swe::Engine;
+using swe::HostInstance;
+
+struct swe_ctx {
+  Engine eng;
+  std::string err;
+  int flux = 1, ws = 2;
+  double cfl = 0.15;
+  bool primed = false;
+};
+
+struct swe_batch {
+  Engine eng;
+  std::string err;
+  bool primed = false;
+};
+
+namespace {
+
+thread_local std::string g_create_error;
+
+swe_status fail(std::string* slot, swe_status st, const std::string& msg) {
+  if (slot) *slot = msg;
+  else g_create_error = msg;
+  return st;
+}
+
+swe_status cuda_fail(std::string* slot, cudaError_t e, const char* where) {
+  return fail(slot, SWE_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+// Interleave / de-interleave between the reference's 3 x C column-major
+// primitive field and the engine's three component arrays.
+__global__ void k_pack(const double* __restrict__ W, const double* __restrict__ U, const double* __restrict__ V,
+                       double* __restrict__ out, int n) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    out[3 * i] = W[i];
+    out[3 * i + 1] = U[i];
+    out[3 * i + 2] = V[i];
+  }
+}
+__global__ void k_unpack(const double* __restrict__ in, double* __restrict__ W, double* __restrict__ U,
+                         double* __restrict__ V, int n) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    W[i] = in[3 * i];
+    U[i] = in[3 * i + 1];
+    V[i] = in[3 * i + 2];
+  }
+}
+
+swe_status read_instance(const swe_mesh* m, const swe_params* p, HostInstance* h, std::string* why) {
+  if (!m || !m->geometry || !m->edge_nodes || !m->edge_cells || !m->cell_nodes || !m->cell_edges ||
+      !m->cell_neighbours) {
+    *why = "mesh or one of its arrays is NULL";
+    return SWE_ERR_INVALID_ARGUMENT;
+  }
+  if (m->num_nodes <= 0 || m->num_edges <= 0 || m->num_cells <= 0) {
+    *why = "mesh sizes must be positive";
+    return SWE_ERR_INVALID_MESH;
+  }
+  if (!(p->cfl > 0.) || !std::isfinite(p->cfl) || !std::isfinite(p->cor)) {
+    *why = "cfl must be positive and finite, cor finite";
+    return SWE_ERR_INVALID_ARGUMENT;
+  }
+  h->C = m->num_cells;
+  h->E = m->num_edges;
+  h->N = m->num_nodes;
+  h->geom.assign(m->geometry, m->geometry + 3 * m->num_nodes);
+  h->en.assign(m->edge_nodes, m->edge_nodes + 2 * m->num_edges);
+  h->ec.assign(m->edge_cells, m->edge_cells + 2 * m->num_edges);
+  h->cn.assign(m->cell_nodes, m->cell_nodes + 3 * m->num_cells);
+  h->ce.assign(m->cell_edges, m->cell_edges + 3 * m->num_cells);
+  h->ct.assign(m->cell_neighbours, m->cell_neighbours + 3 * m->num_cells);
+  h->cfl = p->cfl;
+  h->cor = p->cor;
+  return SWE_OK;
+}
+
+swe_status check_params(const swe_params* p, std::string* why) {
+  if (p->flux < 0 || p->flux > 1) {
+    *why = "flux must be SWE_FLUX_HLL or SWE_FLUX_HLLC";
+    return SWE_ERR_INVALID_ARGUMENT;
+  }
+  if (p->wavespeed < 0 || p->wavespeed > 2) {
+    *why = "wavespeed must be SWE_WS_RUSANOV, SWE_WS_DAVIS or SWE_WS_EINFELDT";
+    return SWE_ERR_INVALID_ARGUMENT;
+  }
+  if (p->reorder != 0) {
+    *why = "reorder: only 0 (the caller's cell order) is implemented";
+    return SWE_ERR_UNSUPPORTED;
+  }
+  return SWE_OK;
+}
+
+swe_status upload_prim(Engine& eng, const double* prim, int64_t c0, int64_t n, std::string* err) {
+  for (int64_t q = 0; q < 3 * n; ++q)
+    if (!std::isfinite(prim[q]))
+      return fail(err, SWE_ERR_NONFINITE, "state has a non-finite value at cell " + std::to_string(q / 3));
+  // one copy of the interleaved field into the staging buffer, then a device unpack
+  cudaError_t e = cudaMemcpyAsync(eng.d_io, prim, 3 * n * sizeof(double), cudaMemcpyHostToDevice, eng.stream());
+  if (e == cudaSuccess) {
+    k_unpack<<<(int)((n + 255) / 256), 256, 0, eng.stream()>>>(eng.d_io, eng.state(0, 0) + c0, eng.state(0, 1) + c0,
+                                                                eng.state(0, 2) + c0, (int)n);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(eng.stream());
+  if (e != cudaSuccess) return cuda_fail(err, e, "uploading the state");
+  return SWE_OK;
+}
+
+swe_status download_prim(Engine& eng, double* prim, int64_t c0, int64_t n, std::string* err) {
+  k_pack<<<(int)((n + 255) / 256), 256, 0, eng.stream()>>>(eng.state(0, 0) + c0, eng.state(0, 1) + c0,
+                                                            eng.state(0, 2) + c0, eng.d_io, (int)n);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(prim, eng.d_io, 3 * n * sizeof(double), cudaMemcpyDeviceToHost, eng.stream());
+  if (e == cudaSuccess) e = cudaStreamSynchronize(eng.stream());
+  if (e != cudaSuccess) return cuda_fail(err, e, "downloading the state");
+  return SWE_OK;
+}
+
+// Reads and clears nothing: reports the device error word.
+swe_status check_device(Engine& eng, std::string* err) {
+  cudaError_t e = cudaStreamSynchronize(eng.stream());
+  if (e != cudaSuccess) return cuda_fail(err, e, "device execution");
+  unsigned flags = 0;
+  e = cudaMemcpy(&flags, eng.work().err, sizeof(unsigned), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(err, e, "reading the device error word");
+  if (flags & swe::kErrNonFinite) return fail(err, SWE_ERR_NONFINITE, "a cell update produced a non-finite value");
+  return SWE_OK;
+}
+
+// Priming flux pass so that CFLdt() is defined before the first step.
+swe_status prime(Engine& eng, std::string* err) {
+  cudaError_t e = eng.reset_pass();
+  if (e == cudaSuccess) e = eng.interface_values(eng.state(0, 0), eng.state(0, 1), eng.state(0, 2), 0);
+  if (e == cudaSuccess) e = eng.fluxes(eng.state(0, 0));
+  if (e == cudaSuccess) e = eng.reset_pass();
+  if (e != cudaSuccess) return cuda_fail(err, e, "priming flux pass");
+  return SWE_OK;
+}
+
+#define SWE_GUARD_BEGIN try {
+#define SWE_GUARD_END(slot)                                           \
+  }                                                                   \
+  catch (const std::bad_alloc&) {                                     \
+    return fail(slot, SWE_ERR_OUT_OF_MEMORY, "host allocation failed"); \
+  }                                                                   \
+  catch (const std::exception& ex) {                                  \
+    return fail(slot, SWE_ERR_INVALID_ARGUMENT, ex.what());           \
+  }
+
+}  // namespace
+
+extern "C" {
+
+swe_status swe_params_default(swe_params* p) {
+  if (!p) return SWE_ERR_INVALID_ARGUMENT;
+  p->flux = SWE_FLUX_HLLC;
+  p->wavespeed = SWE_WS_EINFELDT;
+  p->cor = 0.;
+  p->tau = 0.;
+  p->cfl = 0.15;
+  p->reorder = 0;
+  p->block = 0;
+  return SWE_OK;
+}
+
+swe_status swe_create(const swe_mesh* mesh, const double* prim0, const swe_params* params, swe_ctx** out) {
+  SWE_GUARD_BEGIN
+  if (!out) return fail(nullptr, SWE_ERR_INVALID_ARGUMENT, "out is NULL");
+  *out = nullptr;
+  if (!prim0) return fail(nullptr, SWE_ERR_INVALID_ARGUMENT, "prim0 is NULL");
+  swe_params p;
+  if (params) p = *params;
+  else swe_params_default(&p);
+  std::string why;
+  swe_status st = check_params(&p, &why);
+  if (st != SWE_OK) return fail(nullptr, st, why);
+  std::vector<HostInstance> inst(1);
+  st = read_instance(mesh, &p, &inst[0], &why);
+  if (st != SWE_OK) return fail(nullptr, st, why);
+  std::unique_ptr<swe_ctx> ctx(new swe_ctx());
+  ctx->flux = p.flux;
+  ctx->ws = p.wavespeed;
+  ctx->cfl = p.cfl;
+  int ist = 0;
+  const int64_t C = inst[0].C;
+  std::string e = ctx->eng.init(std::move(inst), p.flux, p.wavespeed, p.block, &ist, false);
+  if (!e.empty()) return fail(nullptr, (swe_status)ist, e);
+  st = upload_prim(ctx->eng, prim0, 0, C, &why);
+  if (st != SWE_OK) return fail(nullptr, st, why);
+  st = prime(ctx->eng, &why);
+  if (st != SWE_OK) return fail(nullptr, st, why);
+  *out = ctx.release();
+  return SWE_OK;
+  SWE_GUARD_END(nullptr)
+}
+
+swe_status swe_destroy(swe_ctx* ctx) {
+  if (!ctx) return SWE_ERR_INVALID_ARGUMENT;
+  cudaStreamSynchronize(ctx->eng.stream());
+  delete ctx;
+  return SWE_OK;
+}
+
+swe_status swe_set_stream(swe_ctx* ctx, void* stream) {
+  if (!ctx) return SWE_ERR_INVALID_ARGUMENT;
+  ctx->eng.set_stream(stream ? (cudaStream_t)stream : nullptr);
+  return SWE_OK;
+}
+
+swe_status swe_step(swe_ctx* ctx, int32_t scheme, double dt) {
+  if (!ctx) return SWE_ERR_INVALID_ARGUMENT;
+  SWE_GUARD_BEGIN
+  if (scheme < 0 || scheme > 2) return fail(&ctx->err, SWE_ERR_INVALID_ARGUMENT, "scheme must be 0, 1 or 2");
+  if (!(dt > 0.) || !std::isfinite(dt)) return fail(&ctx->err, SWE_ERR_INVALID_ARGUMENT, "dt must be positive and finite");
+  cudaError_t e = cudaMemcpyAsync(ctx->eng.d_fixed_dt, &dt, sizeof(double), cudaMemcpyHostToDevice, ctx->eng.stream());
+  if (e == cudaSuccess) e = ctx->eng.step(scheme, 2);
+  if (e != cudaSuccess) return cuda_fail(&ctx->err, e, "swe_step");
+  return SWE_OK;
+  SWE_GUARD_END(&ctx->err)
+}
+
+swe_status swe_run(swe_ctx* ctx, int32_t scheme, double dt, int64_t n_steps) {
+  if (!ctx) return SWE_ERR_INVALID_ARGUMENT;
+  SWE_GUARD_BEGIN
+  if (scheme < 0 || scheme > 2) return fail(&ctx->err, SWE_ERR_INVALID_ARGUMENT, "scheme must be 0, 1 or 2");
+  if (!(dt > 0.) || !std::isfinite(dt)) return fail(&ctx->err, SWE_ERR_INVALID_ARGUMENT, "dt must be positive and finite");
+  if (n_steps < 0) return fail(&ctx->err, SWE_ERR_INVALID_ARGUMENT, "n_steps must be >= 0");
+  cudaError_t e = cudaMemcpyAsync(ctx->eng.d_fixed_dt, &dt, sizeof(double), cudaMemcpyHostToDevice, ctx->eng.stream());
+  if (e == cudaSuccess) e = ctx->eng.run_graph(scheme, 2, n_steps);
+  if (e != cudaSuccess) return cuda_fail(&ctx->err, e, "swe_run");
+  return SWE_OK;
+  SWE_GUARD_END(&ctx->err)
+}
+
+swe_status swe_run_cfl(swe_ctx* ctx, int32_t scheme, int64_t n_steps, double* t_elapsed) {
+  if (!ctx) return SWE_ERR_INVALID_ARGUMENT;
+  SWE_GUARD_BEGIN
+  if (scheme < 0 || scheme > 2) return fail(&ctx->err, SWE_ERR_INVALID_ARGUMENT, "scheme must be 0, 1 or 2");
+  if (n_steps < 0) return fail(&ctx->err, SWE_ERR_INVALID_ARGUMENT, "n_steps must be >= 0");
+  cudaError_t e = ctx->eng.run_graph(scheme, 1, n_steps);
+  if (e != cudaSuccess) return cuda_fail(&ctx->err, e, "swe_run_cfl");
+  if (t_elapsed) {
+    e = cudaMemcpyAsync(t_elapsed, ctx->eng.work().tsum, sizeof(double), cudaMemcpyDeviceToHost, ctx->eng.stream());
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->eng.stream());
+    if (e != cudaSuccess) return cuda_fail(&ctx->err, e, "swe_run_cfl");
+  }
+  return SWE_OK;
+  SWE_GUARD_END(&ctx->err)
+}
+
+swe_status swe_min_len_to_wavespeed(swe_ctx* ctx, double* r) {
+  if (!ctx || !r) return SWE_ERR_INVALID_ARGUMENT;
+  unsigned long long k = 0;
+  cudaError_t e = cudaMemcpyAsync(&k, ctx->eng.work().r, sizeof(k), cudaMemcpyDeviceToHost, ctx->eng.stream());
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->eng.stream());
+  if (e != cudaSuccess) return cuda_fail(&ctx->err, e, "swe_min_len_to_wavespeed");
+  *r = swe::order_val(k);
+  return SWE_OK;
+}
+
+swe_status swe_cfl_dt(swe_ctx* ctx, double* dt) {
+  if (!ctx || !dt) return SWE_ERR_INVALID_ARGUMENT;
+  double r = 0.;
+  swe_status st = swe_min_len_to_wavespeed(ctx, &r);
+  if (st != SWE_OK) return st;
+  *dt = ctx->cfl * r;
+  return SWE_OK;
+}
+
+swe_status swe_compute_interface_values(swe_ctx* ctx) {
+  if (!ctx) return SWE_ERR_INVALID_ARGUMENT;
+  Engine& g = ctx->eng;
+  cudaError_t e = g.reset_pass();
+  if (e == cudaSuccess) e = g.interface_values(g.state(0, 0), g.state(0, 1), g.state(0, 2), 0);
+  if (e != cudaSuccess) return cuda_fail(&ctx->err, e, "swe_compute_interface_values");
+  return SWE_OK;
+}
+
+swe_status swe_compute_fluxes(swe_ctx* ctx) {
+  if (!ctx) return SWE_ERR_INVALID_ARGUMENT;
+  cudaError_t e = ctx->eng.fluxes(ctx->eng.state(0, 0));
+  if (e != cudaSuccess) return cuda_fail(&ctx->err, e, "swe_compute_fluxes");
+  return SWE_OK;
+}
+
+swe_status swe_get_prim(swe_ctx* ctx, double* prim_out) {
+  if (!ctx || !prim_out) return SWE_ERR_INVALID_ARGUMENT;
+  SWE_GUARD_BEGIN
+  return download_prim(ctx->eng, prim_out, 0, ctx->eng.C(), &ctx->err);
+  SWE_GUARD_END(&ctx->err)
+}
+
+swe_status swe_set_prim(swe_ctx* ctx, const double* prim_in) {
+  if (!ctx || !prim_in) return SWE_ERR_INVALID_ARGUMENT;
+  SWE_GUARD_BEGIN
+  // like assigning the reference's volume field: CFLdt() keeps the ratio of
+  // the last flux pass
+  return upload_prim(ctx->eng, prim_in, 0, ctx->eng.C(), &ctx->err);
+  SWE_GUARD_END(&ctx->err)
+}
+
+swe_status swe_get_prim_device(swe_ctx* ctx, double* out) {
+  if (!ctx || !out) return SWE_ERR_INVALID_ARGUMENT;
+  Engine& g = ctx->eng;
+  const int n = g.C();
+  k_pack<<<(n + 255) / 256, 256, 0, g.stream()>>>(g.state(0, 0), g.state(0, 1), g.state(0, 2), out, n);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(&ctx->err, e, "swe_get_prim_device");
+  return SWE_OK;
+}
+
+swe_status swe_set_prim_device(swe_ctx* ctx, const double* in) {
+  if (!ctx || !in) return SWE_ERR_INVALID_ARGUMENT;
+  Engine& g = ctx->eng;
+  const int n = g.C();
+  k_unpack<<<(n + 255) / 256, 256, 0, g.stream()>>>(in, g.state(0, 0), g.state(0, 1), g.state(0, 2), n);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(&ctx->err, e, "swe_set_prim_device");
+  return SWE_OK;
+}
+
+swe_status swe_get_edge_values(swe_ctx* ctx, double* edg_out, double* src_out) {
+  if (!ctx) return SWE_ERR_INVALID_ARGUMENT;
+  SWE_GUARD_BEGIN
+  Engine& g = ctx->eng;
+  const int64_t C = g.C(), E = g.E();
+  std::vector<double> ew(3 * C), eu(3 * C), ev(3 * C), sx(3 * C), sy(3 * C);
+  const swe::DevWork& w = g.work();
+  cudaError_t e = cudaStreamSynchronize(g.stream());
+  if (e == cudaSuccess) e = cudaMemcpy(ew.data(), w.ew, 3 * C * sizeof(double), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(eu.data(), w.eu, 3 * C * sizeof(double), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(ev.data(), w.ev, 3 * C * sizeof(double), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(sx.data(), w.sx, 3 * C * sizeof(double), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(sy.data(), w.sy, 3 * C * sizeof(double), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(&ctx->err, e, "swe_get_edge_values");
+  const HostInstance& h = g.host[0];
+  if (edg_out) std::memset(edg_out, 0, 6 * E * sizeof(double));
+  if (src_out) std::memset(src_out, 0, 6 * E * sizeof(double));
+  for (int64_t i = 0; i < C; ++i)
+    for (int k = 0; k < 3; ++k) {
+      const int64_t ed = h.ce[3 * i + k], nb = h.ct[3 * i + k];
+      const int64_t id = 2 * ed + (i < nb ? 1 : 0);  // EdgeIndexer::Id (include/ValueField.h:70-75)
+      const int64_t s = k * C + i;
+      if (edg_out) {
+        edg_out[3 * id] = ew[s];
+        edg_out[3 * id + 1] = eu[s];
+        edg_out[3 * id + 2] = ev[s];
+      }
+      if (src_out) {
+        src_out[3 * id + 1] = sx[s];
+        src_out[3 * id + 2] = sy[s];
+      }
+    }
+  return SWE_OK;
+  SWE_GUARD_END(&ctx->err)
+}
+
+swe_status swe_get_fluxes(swe_ctx* ctx, double* f_out) {
+  if (!ctx || !f_out) return SWE_ERR_INVALID_ARGUMENT;
+  SWE_GUARD_BEGIN
+  Engine& g = ctx->eng;
+  const int64_t E = g.E();
+  std::vector<double> a(E), b(E), c(E);
+  cudaError_t e = cudaStreamSynchronize(g.stream());
+  if (e == cudaSuccess) e = cudaMemcpy(a.data(), g.work().f0, E * sizeof(double), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(b.data(), g.work().f1, E * sizeof(double), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(c.data(), g.work().f2, E * sizeof(double), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(&ctx->err, e, "swe_get_fluxes");
+  for (int64_t q = 0; q < E; ++q) {
+    f_out[3 * q] = a[q];
+    f_out[3 * q + 1] = b[q];
+    f_out[3 * q + 2] = c[q];
+  }
+  return SWE_OK;
+  SWE_GUARD_END(&ctx->err)
+}
+
+swe_status swe_get_node_max(swe_ctx* ctx, double* max_out) {
+  if (!ctx || !max_out) return SWE_ERR_INVALID_ARGUMENT;
+  SWE_GUARD_BEGIN
+  Engine& g = ctx->eng;
+  const int64_t N = g.N();
+  std::vector<unsigned long long> k(N);
+  cudaError_t e = cudaStreamSynchronize(g.stream());
+  if (e == cudaSuccess) e = cudaMemcpy(k.data(), g.work().maxwp, N * sizeof(k[0]), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(&ctx->err, e, "swe_get_node_max");
+  for (int64_t q = 0; q < N; ++q) max_out[q] = swe::order_val(k[q]);
+  return SWE_OK;
+  SWE_GUARD_END(&ctx->err)
+}
+
+swe_status swe_time_kernels(swe_ctx* ctx, int32_t scheme, int64_t reps, double* out_ms) {
+  if (!ctx || !out_ms) return SWE_ERR_INVALID_ARGUMENT;
+  if (scheme < 0 || scheme > 2 || reps <= 0) return fail(&ctx->err, SWE_ERR_INVALID_ARGUMENT, "bad scheme or reps");
+  double acc[6] = {0, 0, 0, 0, 0, 0};
+  for (int64_t r = 0; r < reps; ++r) {
+    cudaError_t e = ctx->eng.step_timed(scheme, 1, acc);
+    if (e != cudaSuccess) return cuda_fail(&ctx->err, e, "swe_time_kernels");
+  }
+  const int n_st = swe::scheme_table(scheme).n;
+  for (int k = 0; k < 5; ++k) out_ms[k] = acc[k] / (double)(reps * n_st);
+  out_ms[5] = acc[5] / (double)reps;
+  return SWE_OK;
+}
+
+swe_status swe_num_cells(swe_ctx* ctx, int64_t* n) {
+  if (!ctx || !n) return SWE_ERR_INVALID_ARGUMENT;
+  *n = ctx->eng.C();
+  return SWE_OK;
+}
+
+swe_status swe_launch_count(swe_ctx* ctx, int64_t* n) {
+  if (!ctx || !n) return SWE_ERR_INVALID_ARGUMENT;
+  *n = ctx->eng.launches();
+  return SWE_OK;
+}
+
+swe_status swe_synchronize(swe_ctx* ctx) {
+  if (!ctx) return SWE_ERR_INVALID_ARGUMENT;
+  return check_device(ctx->eng, &ctx->err);
+}
+
+const char* swe_last_error(swe_ctx* ctx) {
+  if (!ctx) return g_create_error.c_str();
+  return ctx->err.c_str();
+}
+
+// ------------------------------------------------------------------ batched
+swe_status swe_batch_create(int32_t n_instances, const swe_mesh* meshes, const double* const* prim0,
+                            const swe_params* params, int32_t n_params, swe_batch** out) {
+  SWE_GUARD_BEGIN
+  if (!out) return fail(nullptr, SWE_ERR_INVALID_ARGUMENT, "out is NULL");
+  *out = nullptr;
+  if (n_instances <= 0 || !meshes || !prim0) return fail(nullptr, SWE_ERR_INVALID_ARGUMENT, "no instances");
+  if (params && n_params != 1 && n_params != n_instances)
+    return fail(nullptr, SWE_ERR_INVALID_ARGUMENT, "n_params must be 1 or n_instances");
+  std::vector<HostInstance> inst(n_instances);
+  swe_params p0;
+  swe_params_default(&p0);
+  if (params) p0 = params[0];
+  std::string why;
+  for (int q = 0; q < n_instances; ++q) {
+    swe_params p = p0;
+    if (params && n_params == n_instances) p = params[q];
+    swe_status st = check_params(&p, &why);
+    if (st != SWE_OK) return fail(nullptr, st, "instance " + std::to_string(q) + ": " + why);
+    if (p.flux != p0.flux || p.wavespeed != p0.wavespeed)
+      return fail(nullptr, SWE_ERR_UNSUPPORTED, "all instances of a batch must use the same flux and wave speed");
+    if (!prim0[q]) return fail(nullptr, SWE_ERR_INVALID_ARGUMENT, "prim0[" + std::to_string(q) + "] is NULL");
+    st = read_instance(&meshes[q], &p, &inst[q], &why);
+    if (st != SWE_OK) return fail(nullptr, st, "instance " + std::to_string(q) + ": " + why);
+  }
+  std::unique_ptr<swe_batch> b(new swe_batch());
+  int ist = 0;
+  std::string e = b->eng.init(std::move(inst), p0.flux, p0.wavespeed, p0.block, &ist, true);
+  if (!e.empty()) return fail(nullptr, (swe_status)ist, e);
+  for (int q = 0; q < n_instances; ++q) {
+    const int64_t c0 = b->eng.cell_off[q], n = b->eng.cell_off[q + 1] - c0;
+    swe_status st = upload_prim(b->eng, prim0[q], c0, n, &why);
+    if (st != SWE_OK) return fail(nullptr, st, "instance " + std::to_string(q) + ": " + why);
+  }
+  swe_status st = prime(b->eng, &why);
+  if (st != SWE_OK) return fail(nullptr, st, why);
+  *out = b.release();
+  return SWE_OK;
+  SWE_GUARD_END(nullptr)
+}
+
+swe_status swe_batch_destroy(swe_batch* b) {
+  if (!b) return SWE_ERR_INVALID_ARGUMENT;
+  cudaStreamSynchronize(b->eng.stream());
+  delete b;
+  return SWE_OK;
+}
+
+swe_status swe_batch_run_cfl(swe_batch* b, int32_t scheme, int64_t n_steps) {
+  if (!b) return SWE_ERR_INVALID_ARGUMENT;
+  if (scheme < 0 || scheme > 2 || n_steps < 0) return fail(&b->err, SWE_ERR_INVALID_ARGUMENT, "bad scheme or n_steps");
+  cudaError_t e = b->eng.run_graph(scheme, 1, n_steps);
+  if (e != cudaSuccess) return cuda_fail(&b->err, e, "swe_batch_run_cfl");
+  return SWE_OK;
+}
+
+swe_status swe_batch_run(swe_batch* b, int32_t scheme, double dt, int64_t n_steps) {
+  if (!b) return SWE_ERR_INVALID_ARGUMENT;
+  if (scheme < 0 || scheme > 2 || n_steps < 0) return fail(&b->err, SWE_ERR_INVALID_ARGUMENT, "bad scheme or n_steps");
+  if (!(dt > 0.) || !std::isfinite(dt)) return fail(&b->err, SWE_ERR_INVALID_ARGUMENT, "dt must be positive and finite");
+  cudaError_t e = cudaMemcpyAsync(b->eng.d_fixed_dt, &dt, sizeof(double), cudaMemcpyHostToDevice, b->eng.stream());
+  if (e == cudaSuccess) e = b->eng.run_graph(scheme, 2, n_steps);
+  if (e != cudaSuccess) return cuda_fail(&b->err, e, "swe_batch_run");
+  return SWE_OK;
+}
+
+swe_status swe_batch_get_prim(swe_batch* b, int32_t q, double* prim_out) {
+  if (!b || !prim_out || q < 0 || q >= b->eng.I()) return SWE_ERR_INVALID_ARGUMENT;
+  SWE_GUARD_BEGIN
+  const int64_t c0 = b->eng.cell_off[q], n = b->eng.cell_off[q + 1] - c0;
+  return download_prim(b->eng, prim_out, c0, n, &b->err);
+  SWE_GUARD_END(&b->err)
+}
+
+swe_status swe_batch_time(swe_batch* b, int32_t q, double* t) {
+  if (!b || !t || q < 0 || q >= b->eng.I()) return SWE_ERR_INVALID_ARGUMENT;
+  cudaError_t e = cudaMemcpyAsync(t, b->eng.work().tsum + q, sizeof(double), cudaMemcpyDeviceToHost, b->eng.stream());
+  if (e == cudaSuccess) e = cudaStreamSynchronize(b->eng.stream());
+  if (e != cudaSuccess) return cuda_fail(&b->err, e, "swe_batch_time");
+  return SWE_OK;
+}
+
+swe_status swe_batch_launch_count(swe_batch* b, int64_t* n) {
+  if (!b || !n) return SWE_ERR_INVALID_ARGUMENT;
+  *n = b->eng.launches();
+  return SWE_OK;
+}
+
+swe_status swe_batch_synchronize(swe_batch* b) {
+  if (!b) return SWE_ERR_INVALID_ARGUMENT;
+  return check_device(b->eng, &b->err);
+}
+
+const char* swe_batch_last_error(swe_batch* b) {
+  if (!b) return g_create_error.c_str();
+  return b->err.c_str();
+}
+
+}  // extern "C"

@@ -1,0 +1,202 @@
+// swe_engine.cuh -- device data layout and the engine that owns it.
+//
+// Layout in HBM (all indices int32, all values FP64, structure of arrays):
+//   cells  : C = sum of the instances' cells, concatenated instance by instance
+//   edges  : E, likewise; nodes: N, likewise
+//   "slot" (i, k) = interface value of cell i on its local edge k, stored at
+//   k * C + i, so a warp writes and reads its own cells' slots coalesced.
+// Static per-cell records hold every quantity of the reference step that
+// depends on the mesh alone (precomputed once on the host with the reference's
+// operation order); the kernels do only state-dependent arithmetic.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "swe_physics.cuh"
+
+namespace swe {
+
+constexpr int kComboStride = 12;  // doubles per full-wet combination record
+constexpr int kPw1Stride = 12;    // doubles per PartWet1 record
+constexpr int kDryStride = 8;     // doubles per dry-cell record
+
+enum : unsigned { kErrNonFinite = 1u, kErrBadState = 2u };
+
+// PartWet2 (src/MUSCLObject.cpp:114-191) geometry: vertices sorted by z.
+struct Pw2Rec {
+  double p[3][3];     // sorted vertices (x, y, z), lowest first
+  double ratio_b;     // (b12 - b23) / (b13 - b23)
+  double hd2f;        // 2 b13 - b12 - b23
+  double d13;         // b13 - b23
+  double beta;        // (b13 - b12) / (b13 - b23)
+  double tp0x, tp0y;  // T - P_lowest
+  double dnode[3][2]; // P_k - T, cell node order
+  double dedge[3][2]; // E_k - T, cell edge order
+  int lo;             // global id of the lowest node
+  int flat;           // b13 - b23 < tol
+};
+
+struct DevMesh {
+  int C, E, N, I;
+  // cells
+  const int* cnode;           // [3][C]
+  const int* cnbr;            // [3][C], -1 = wall
+  const int* cedge;           // [3][C]
+  const unsigned char* cown;  // [C] bit k: this cell owns edge k
+  const double* bc;           // [C] centroid bathymetry
+  const double* fwthr;        // [C] max node z, +inf for boundary cells
+  const double* area;         // [C]
+  const double* zn;           // [3][C] node z
+  const double* ze;           // [3][C] edge-centre z
+  const double* cek;          // [3][C] L(e_k) / A
+  const double* cnx;          // [3][C] outward normal of edge k
+  const double* cny;          // [3][C]
+  const double* dry;          // [C][8] dry-cell node/edge values and slope
+  const double* combo;        // [C][8][12] full-wet plane records
+  const double* pw1;          // [C][12]
+  const Pw2Rec* pw2;          // [C]
+  const int* cinst;           // [C] instance of the cell (batched only)
+  // edges
+  const int* eown;    // [E]
+  const int* enb;     // [E] -1 = wall
+  const int* eslotl;  // [E] slot of the owner's interface value
+  const int* eslotr;  // [E] slot of the neighbour's interface value
+  const double* enx;
+  const double* eny;
+  const double* etx;
+  const double* ety;
+  const double* ezm;    // edge-centre bathymetry
+  const double* elmin;  // min(2A_owner/L, 2A_nb/L)
+  const int* einst;     // [E] (batched only)
+  // nodes
+  const double* nz;  // [N]
+  // instances
+  const int* inst_cell_begin;  // [I]
+  const double* inst_cfl;      // [I]
+  const double* inst_cor;      // [I]
+};
+
+struct DevWork {
+  double* ew;  // [3][C] interface w
+  double* eu;
+  double* ev;
+  double* sx;  // [3][C] source gradient
+  double* sy;
+  double* f0;  // [E] fluxes
+  double* f1;
+  double* f2;
+  double* drain;               // [C] draining time step
+  unsigned long long* maxwp;   // [N] ordered keys of the node maxima
+  int* pwlist;                 // [C] partially-wet cells of this stage
+  int* pwcount;                // [1]
+  double* pwrec;               // [C] PartWet1 level of listed cells
+  unsigned long long* r;       // [I] ordered key of min length-to-wavespeed
+  double* dt;                  // [I] step dt
+  double* tsum;                // [I] accumulated time
+  const double* fixed_dt;      // [1] dt for fixed-step runs
+  unsigned* err;               // [1] error bits
+};
+
+// One Runge-Kutta stage in Shu-Osher form (src/Solvers.cpp:5-59).
+struct Stage {
+  bool first;     // U = U0.cons + RHS(dt)
+  double a, b, c; // U = a U0.cons + b Uprev.cons + RHS(c dt)
+};
+
+struct Scheme {
+  int n;
+  Stage s[3];
+};
+Scheme scheme_table(int scheme);
+
+// Host-side description of one instance after validation.
+struct HostInstance {
+  int64_t C, E, N;
+  std::vector<double> geom;
+  std::vector<int64_t> en, ec, cn, ce, ct;
+  double cfl, cor;
+};
+
+class Engine {
+ public:
+  Engine() = default;
+  ~Engine();
+  // Validates and precomputes every instance, uploads, allocates work arrays.
+  // Returns an empty string on success, else the error message (status in *st).
+  std::string init(std::vector<HostInstance>&& inst, int flux, int ws, int block, int* st, bool batched);
+
+  // NULL selects the engine's own non-blocking stream.
+  void set_stream(cudaStream_t s) { stream_ = s ? s : own_stream_; }
+  cudaStream_t stream() const { return stream_; }
+
+  // Resets the node maxima and the part-wet list (done by k_drain at the end
+  // of every stage; needed before a standalone reconstruction).
+  cudaError_t reset_pass();
+  // Launches one reconstruction (pass 1 + pass 2) and one flux pass.
+  cudaError_t interface_values(const double* W, const double* U, const double* V, int latch_mode);
+  cudaError_t fluxes(const double* W);
+  // One whole step of `scheme`; latch_mode 1 = CFL dt, 2 = fixed dt from
+  // work.fixed_dt.  Enqueued on the engine's stream.
+  cudaError_t step(int scheme, int latch_mode);
+  // n steps through a cached CUDA graph of one step.
+  cudaError_t run_graph(int scheme, int latch_mode, int64_t n);
+  // One step launched kernel by kernel with CUDA events between them;
+  // adds the durations (ms) of k_recon1, k_recon2, k_flux, k_drain, k_update
+  // to acc[0..4] and the whole step to acc[5].  Synchronises.
+  cudaError_t step_timed(int scheme, int latch_mode, double* acc);
+
+  int C() const { return mesh_.C; }
+  int E() const { return mesh_.E; }
+  int N() const { return mesh_.N; }
+  int I() const { return mesh_.I; }
+  int64_t launches() const { return launches_; }
+  double* state(int buf, int comp) { return state_[buf * 3 + comp]; }
+  const DevWork& work() const { return work_; }
+  DevWork& work() { return work_; }
+  const DevMesh& mesh() const { return mesh_; }
+
+  // Instance ranges in the concatenated arrays.
+  std::vector<int64_t> cell_off, edge_off, node_off;
+  // Host copies of the per-instance topology needed by the layout getters.
+  std::vector<HostInstance> host;
+  double* d_io = nullptr;        // [3C] staging buffer for the interleaved 3 x C field
+  double* d_fixed_dt = nullptr;  // device scalar
+  double* h_fixed_dt = nullptr;  // pinned host scalar
+
+ private:
+  cudaError_t launch_stage(const Stage& st, const double* const* in, const double* const* u0, double* const* out,
+                           bool first_stage_of_step, int latch_mode, cudaEvent_t* ev = nullptr);
+  template <class T>
+  T* dalloc(size_t n);
+
+  DevMesh mesh_{};
+  DevWork work_{};
+  double* state_[6] = {};
+  std::vector<void*> allocs_;
+  cudaStream_t stream_ = nullptr;
+  cudaStream_t own_stream_ = nullptr;
+  int flux_ = 1, ws_ = 2, block_ = 256;
+  bool batched_ = false;
+  int64_t launches_ = 0;
+  cudaGraphExec_t graphs_[3][3] = {};
+};
+
+// Precompute (swe_precompute.cu): fills the host images of DevMesh arrays for
+// instance `inst` at offsets (c0, e0, n0) of the concatenated arrays.
+struct HostImage {
+  int C, E, N, I;
+  std::vector<int> cnode, cnbr, cedge, cinst, eown, enb, eslotl, eslotr, einst, inst_cell_begin;
+  std::vector<unsigned char> cown;
+  std::vector<double> bc, fwthr, area, zn, ze, cek, cnx, cny, dry, combo, pw1, enx, eny, etx, ety, ezm, elmin, nz,
+      inst_cfl, inst_cor;
+  std::vector<Pw2Rec> pw2;
+  void resize(int C_, int E_, int N_, int I_);
+};
+std::string validate_instance(const HostInstance& h);
+void precompute_instance(const HostInstance& h, int inst, int64_t c0, int64_t e0, int64_t n0, HostImage& img);
+
+}  // namespace swe

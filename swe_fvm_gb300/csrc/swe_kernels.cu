@@ -1,0 +1,759 @@
+// swe_kernels.cu -- sm_103a kernels of one Runge-Kutta stage and the engine
+// that sequences them.
+//
+// A stage (src/Solvers.cpp:5-59) is five kernels over the concatenated cells
+// and edges of every instance:
+//   k_recon1  all cells    SpaceDisc::ComputeInterfaceValues pass 1
+//                          (src/SpaceDisc.cpp:37-45) + node maxima
+//   k_recon2  part-wet     pass 2 (src/SpaceDisc.cpp:47-51), reading the
+//                          pass-1 node maxima only (order-independent)
+//   k_flux    all edges    SpaceDisc::ComputeFluxes (src/SpaceDisc.cpp:54-74)
+//                          with the flux plugin and the CFL min-reduction
+//   k_drain   all cells    TimeDisc::ComputeDrainingDt (src/TimeDisc.cpp:43-66),
+//                          once per cell instead of 4x per RHS
+//   k_update  all cells    TimeDisc::RHS + ConsAssigner (src/TimeDisc.cpp:3-41,
+//                          src/Assigners.cpp:28-44), an edge-to-cell gather
+// Every read of a stage comes from the start-of-stage state, so results do not
+// depend on the cell order or on scheduling; the only atomics (node maxima,
+// CFL minimum, part-wet list append) are exact max/min/append operations.
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <string>
+
+#include "swe_engine.cuh"
+
+namespace swe {
+
+Scheme scheme_table(int scheme) {
+  Scheme s{};
+  s.s[0] = Stage{true, 0., 0., 1.};
+  if (scheme == 0) {
+    s.n = 1;
+  } else if (scheme == 1) {
+    s.n = 2;
+    s.s[1] = Stage{false, 0.5, 0.5, 0.5};
+  } else {
+    s.n = 3;
+    s.s[1] = Stage{false, 0.75, 0.25, 0.25};
+    s.s[2] = Stage{false, 1. / 3., 2. / 3., 2. / 3.};
+  }
+  return s;
+}
+
+namespace {
+
+constexpr double kInf = __builtin_huge_val();
+
+__device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }
+
+// ------------------------------------------------------------ interface write
+// UpdateInterfaceValues for one edge slot (src/SpaceDisc.cpp:24-29): AtPoint
+// value (w, u, v) already dry-checked, through PrimAssigner with the edge
+// bathymetry, plus the source gradient and Coriolis term.
+__device__ __forceinline__ void write_slot(const DevWork& wk, int slot, double be, double w, double u, double v,
+                                           double gx, double gy, double cor) {
+  double ow, ou, ov;
+  prim_assign(be, w, u, v, &ow, &ou, &ov);
+  wk.ew[slot] = ow;
+  wk.eu[slot] = ou;
+  wk.ev[slot] = ov;
+  double sx = gx, sy = gy;
+  sx += cor * (-ov);
+  sy += cor * ou;
+  wk.sx[slot] = sx;
+  wk.sy[slot] = sy;
+}
+
+// MUSCL::AtPoint with a w-only plane (include/MUSCLObject.h:26-33): the value
+// at a point whose offset term is `off` and whose bathymetry is z.
+__device__ __forceinline__ bool at_point_wet(double w0, double off, double z, double* wout) {
+  double a = w0 + off;
+  if ((a - z) >= 0) {
+    *wout = a;
+    return true;
+  }
+  *wout = z;
+  return false;
+}
+
+__device__ __forceinline__ void node_max(const DevWork& wk, int node, double val, double z) {
+  // max_wp starts at the node z and every AtPoint value is >= z, so values
+  // equal to z cannot raise it.
+  if (val != z) atomicMax(wk.maxwp + node, order_key(val));
+}
+
+// PartWet1 level (src/MUSCLObject.cpp:86-112)
+__device__ __forceinline__ double partwet1_level(const double* __restrict__ p, double w, double h) {
+  const double b13 = p[0], b23 = p[1], b12 = p[2], bdel = p[3];
+  if (w >= b13) return w;
+  if (w <= bdel) return b23 + cbrt(3. * h * p[6] * p[7]);
+  double cc = p[6] * (3. * h * p[8] - p[9]) - p[10];
+  (void)b12;
+  return bisection(cc, p[5], p[4], p[2], b13);
+}
+
+// ---------------------------------------------------------------- kernels
+template <bool BATCH>
+__global__ void __launch_bounds__(256) k_recon1(DevMesh m, DevWork wk, const double* __restrict__ W,
+                                                const double* __restrict__ U, const double* __restrict__ V,
+                                                int latch_mode) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  bool part = false;
+  if (i < m.C) {
+    const int inst = BATCH ? m.cinst[i] : 0;
+    if (i == (BATCH ? m.inst_cell_begin[inst] : 0)) {
+      if (latch_mode == 1) {  // dt = TimeDisc::CFLdt() of the previous flux pass
+        double dt = m.inst_cfl[inst] * order_val(wk.r[inst]);
+        wk.dt[inst] = dt;
+        wk.tsum[inst] += dt;
+      } else if (latch_mode == 2) {
+        double dt = *wk.fixed_dt;
+        wk.dt[inst] = dt;
+        wk.tsum[inst] += dt;
+      }
+      wk.r[inst] = order_key(1.0);  // src/SpaceDisc.cpp:56
+    }
+    const int C = m.C;
+    const double cor = m.inst_cor[inst];
+    const double w = W[i], u = U[i], v = V[i];
+    const double h = w - m.bc[i];
+    if (!is_wet(h)) {
+      // ReconstructDryCell: every value is a mesh constant
+      const double* dr = m.dry + (size_t)i * kDryStride;
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        node_max(wk, m.cnode[k * C + i], dr[k], m.zn[k * C + i]);
+        const int slot = k * C + i;
+        write_slot(wk, slot, m.ze[slot], dr[3 + k], 0., 0., dr[6], dr[7], cor);
+      }
+    } else if (!(m.fwthr[i] < w)) {
+      // partially wet: PartWet1 now (node maxima), PartWet2 in k_recon2
+      const double* p = m.pw1 + (size_t)i * kPw1Stride;
+      const double wr = partwet1_level(p, w, h);
+      wk.pwrec[i] = wr;
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const double z = m.zn[k * C + i];
+        double val;
+        at_point_wet(wr, 0., z, &val);
+        node_max(wk, m.cnode[k * C + i], val, z);
+      }
+      part = true;
+    } else {
+      // ReconstructFullWetCell (src/MUSCLObject.cpp:38-84)
+      int mask = 0;
+      bool first_order = false;
+      double wn[3];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const int nb = m.cnbr[k * C + i];  // never a wall: fully-wet cells are interior
+        const double wj = W[nb];
+        wn[k] = wj;
+        if (m.fwthr[nb] < wj) {
+          // fully-wet neighbour: plane point at its centroid
+        } else if (!is_wet(wj - m.bc[nb])) {
+          first_order = true;
+        } else {
+          mask |= 1 << k;  // partially-wet neighbour: plane point at the edge centre
+        }
+      }
+      double gx = 0., gy = 0.;
+      double toff[3] = {0., 0., 0.}, noff[3] = {0., 0., 0.};
+      if (!first_order) {
+        const double* rec = m.combo + ((size_t)i * 8 + mask) * kComboStride;
+        const double g0 = rec[0], g1 = rec[1];
+        bool pos = true;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          const double hp = (rec[2 + k] + w) - m.zn[k * C + i];
+          if (!is_wet(hp)) pos = false;
+        }
+        if (pos) {
+          // binary TVD limiter on the w row (rows u, v of df are zero)
+          bool tvd = true;
+#pragma unroll
+          for (int k = 0; k < 3; ++k) {
+            const double vmin = smin(w, wn[k]), vmax = smax(w, wn[k]);
+            const double vek = w + rec[5 + k];
+            if (!((vmin <= vek) && (vek <= vmax))) tvd = false;
+          }
+          if (tvd) {
+            gx = g0;
+            gy = g1;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+              toff[k] = rec[5 + k];
+              noff[k] = rec[8 + k];
+            }
+          } else {
+            gx = 0. * g0;  // diag(TVD) * df keeps the sign of zero
+            gy = 0. * g1;
+          }
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const int slot = k * C + i;
+        const double zk = m.zn[slot];
+        double val;
+        at_point_wet(w, noff[k], zk, &val);
+        node_max(wk, m.cnode[slot], val, zk);
+        const double be = m.ze[slot];
+        double we;
+        if (at_point_wet(w, toff[k], be, &we)) write_slot(wk, slot, be, we, u, v, gx, gy, cor);
+        else write_slot(wk, slot, be, we, 0., 0., gx, gy, cor);
+      }
+    }
+  }
+  // warp-aggregated append of the partially-wet cells
+  const unsigned bal = __ballot_sync(0xffffffffu, part);
+  if (bal) {
+    const int leader = __ffs(bal) - 1;
+    int base = 0;
+    if (lane_id() == leader) base = atomicAdd(wk.pwcount, __popc(bal));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    const int slot = base + __popc(bal & ((1u << lane_id()) - 1u));
+    if (part && slot < m.C) wk.pwlist[slot] = i;
+  }
+}
+
+// ReconstructPartWetCell2 (src/MUSCLObject.cpp:114-191) over the listed cells.
+template <bool BATCH>
+__global__ void __launch_bounds__(256) k_recon2(DevMesh m, DevWork wk, const double* __restrict__ W,
+                                                const double* __restrict__ U, const double* __restrict__ V) {
+  const int n = *wk.pwcount;
+  const int C = m.C;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+    const int i = wk.pwlist[q];
+    const int inst = BATCH ? m.cinst[i] : 0;
+    const double cor = m.inst_cor[inst];
+    const double w = W[i], u = U[i], v = V[i];
+    const Pw2Rec& r = m.pw2[i];
+    const double b23 = r.p[0][2], b12 = r.p[1][2], b13 = r.p[2][2];
+    double w0 = wk.pwrec[i];  // PartWet1 fallback level
+    double gx = 0., gy = 0.;
+    bool plane = false;
+    if (!((w > b13) || r.flat)) {
+      const double w23 = order_val(wk.maxwp[r.lo]);
+      const double h23 = w23 - b23;
+      const double ratio_b = r.ratio_b;
+      const double h_delim1 = 1. / 3. * h23 * ratio_b;
+      const double h_delim2 = 1. / 3. * h23 * r.hd2f / r.d13;
+      const double hi = w - m.bc[i];
+      const double ratio_h = hi / h23;
+      // columns of the reference's `points` after all its writes: point 0 is
+      // the lowest vertex with its bathymetry (see the restatement's notes)
+      double p1x, p1y, p1z, p2x, p2y, p2z;
+      bool ok = true;
+      if (hi <= h_delim1) {
+        const double k2 = sqrt(3. * ratio_h / ratio_b);
+        p1x = k2 * r.p[1][0] + (1. - k2) * r.p[0][0];
+        p1y = k2 * r.p[1][1] + (1. - k2) * r.p[0][1];
+        p1z = k2 * r.p[1][2] + (1. - k2) * r.p[0][2];
+        const double k3 = sqrt(3. * ratio_h * ratio_b);
+        p2x = k3 * r.p[2][0] + (1. - k3) * r.p[0][0];
+        p2y = k3 * r.p[2][1] + (1. - k3) * r.p[0][1];
+        p2z = k3 * r.p[2][2] + (1. - k3) * r.p[0][2];
+      } else if (hi >= h_delim2) {
+        const double delta_w = 1.5 * (hi - h_delim2);
+        p1x = r.p[1][0]; p1y = r.p[1][1]; p1z = r.p[1][2];
+        p2x = r.p[2][0]; p2y = r.p[2][1]; p2z = r.p[2][2];
+        p2z += delta_w;
+      } else {
+        const double alpha = 3. * ratio_h;
+        const double beta = r.beta;
+        const double k1 = 1. - bisection((1. + beta - alpha) / (beta * beta), (alpha - 3.) / beta, 0., 0., 1.);
+        if (k1 < kTol) {
+          ok = false;
+        } else {
+          const double bp1 = k1 * b13 + (1. - k1) * b12;
+          p1x = r.p[1][0]; p1y = r.p[1][1]; p1z = r.p[1][2];
+          p2x = k1 * r.p[2][0] + (1. - k1) * r.p[1][0];
+          p2y = k1 * r.p[2][1] + (1. - k1) * r.p[1][1];
+          p2z = bp1;
+        }
+      }
+      if (ok) {
+        plane_gradient(r.p[0][0], r.p[0][1], r.p[0][2], p1x, p1y, p1z, p2x, p2y, p2z, &gx, &gy);
+        w0 = w23 + (gx * r.tp0x + gy * r.tp0y);
+        plane = true;
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const int slot = k * C + i;
+      const double be = m.ze[slot];
+      const double off = plane ? (gx * r.dedge[k][0] + gy * r.dedge[k][1]) : 0.;
+      double we;
+      if (at_point_wet(w0, off, be, &we)) write_slot(wk, slot, be, we, u, v, gx, gy, cor);
+      else write_slot(wk, slot, be, we, 0., 0., gx, gy, cor);
+    }
+  }
+}
+
+// SpaceDisc::ComputeFluxes with flux plugin FLUX and the CFL min-reduction.
+template <class FLUX, bool BATCH>
+__global__ void __launch_bounds__(256) k_flux(DevMesh m, DevWork wk, const double* __restrict__ W) {
+  __shared__ double s_min[32];
+  __shared__ int s_inst[32];
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  double lw = kInf;
+  int inst = 0;
+  if (e < m.E) {
+    if (BATCH) inst = m.einst[e];
+    const int o = m.eown[e];
+    const int nb = m.enb[e];
+    double F[3];
+    const double nx = m.enx[e], ny = m.eny[e];
+    if (nb < 0) {
+      // solid wall: ElemFlux with the owner's cell-average depth (src/SpaceDisc.cpp:66-69)
+      elem_flux(nx, ny, W[o] - m.bc[o], 0., 0., F);
+    } else {
+      EdgeGeom g;
+      g.nx = nx; g.ny = ny;
+      g.tx = m.etx[e]; g.ty = m.ety[e];
+      g.b = m.ezm[e];
+      g.lmin = m.elmin[e];
+      const int sl = m.eslotl[e], sr = m.eslotr[e];
+      SideState L{wk.ew[sl], wk.eu[sl], wk.ev[sl]};
+      SideState R{wk.ew[sr], wk.eu[sr], wk.ev[sr]};
+      FLUX::eval(g, L, R, m.inst_cor[inst], &lw, F);
+    }
+    wk.f0[e] = F[0];
+    wk.f1[e] = F[1];
+    wk.f2[e] = F[2];
+  }
+  // min-reduction of the length-to-wavespeed ratio: warp, block, one atomic
+  const int lane = lane_id(), warp = threadIdx.x >> 5;
+  const int inst0 = __shfl_sync(0xffffffffu, inst, 0);
+  const bool warp_uniform = __all_sync(0xffffffffu, inst == inst0);
+  if (warp_uniform) {
+#pragma unroll
+    for (int off = 16; off; off >>= 1) lw = smin(lw, __shfl_xor_sync(0xffffffffu, lw, off));
+    if (lane == 0) {
+      s_min[warp] = lw;
+      s_inst[warp] = inst0;
+    }
+  } else {
+    if (lw < kInf) atomicMin(wk.r + inst, order_key(lw));
+    if (lane == 0) {
+      s_min[warp] = kInf;
+      s_inst[warp] = -1;
+    }
+  }
+  __syncthreads();
+  if (warp == 0) {
+    const int nw = blockDim.x >> 5;
+    double v = lane < nw ? s_min[lane] : kInf;
+    int vi = lane < nw ? s_inst[lane] : s_inst[0];
+    const int vi0 = __shfl_sync(0xffffffffu, vi, 0);
+    const bool uni = __all_sync(0xffffffffu, vi == vi0 || v == kInf);
+    if (uni) {
+#pragma unroll
+      for (int off = 16; off; off >>= 1) v = smin(v, __shfl_xor_sync(0xffffffffu, v, off));
+      if (lane == 0 && v < kInf) atomicMin(wk.r + vi0, order_key(v));
+    } else if (v < kInf && vi >= 0) {
+      atomicMin(wk.r + vi, order_key(v));
+    }
+  }
+}
+
+// TimeDisc::ComputeDrainingDt once per cell; also resets the node maxima for
+// the next reconstruction.
+__global__ void __launch_bounds__(256) k_drain(DevMesh m, DevWork wk, const double* __restrict__ W) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  // the next pass 1 starts from node z and an empty part-wet list
+  if (i < m.N) wk.maxwp[i] = order_key(m.nz[i]);
+  if (i == 0) *wk.pwcount = 0;
+  if (i >= m.C) return;
+  const double h = W[i] - m.bc[i];
+  double d;
+  if (!is_wet(h)) {
+    d = 0.;
+  } else {
+    const unsigned own = m.cown[i];
+    double sum = 0.;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const double f = wk.f0[m.cedge[k * m.C + i]];
+      sum += smax(0., ((own >> k) & 1u) ? f : -f);
+    }
+    d = sum > kTol ? m.area[i] * h / sum : kInf;
+  }
+  wk.drain[i] = d;
+}
+
+// TimeDisc::RHS + the Shu-Osher combination + ConsAssigner.
+template <bool BATCH>
+// The output may be the same array as Wp or W0 (in-place stages): each thread
+// reads its own cell before writing it, so no pointer here is __restrict__.
+__global__ void __launch_bounds__(256) k_update(DevMesh m, DevWork wk, const double* Wp, const double* Up,
+                                                const double* Vp, const double* W0, const double* U0,
+                                                const double* V0, double* Wo, double* Uo, double* Vo, Stage st) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m.C) return;
+  const int C = m.C;
+  const int inst = BATCH ? m.cinst[i] : 0;
+  const double dt = st.first ? wk.dt[inst] : st.c * wk.dt[inst];
+  const unsigned own = m.cown[i];
+  const double dti = wk.drain[i];
+  double r0 = 0., r1 = 0., r2 = 0.;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const int slot = k * C + i;
+    const int e = m.cedge[slot];
+    const double sgn = ((own >> k) & 1u) ? 1. : -1.;
+    const double F0 = wk.f0[e], F1 = wk.f1[e], F2 = wk.f2[e];
+    const int nb = m.cnbr[slot];
+    const double dtik = nb < 0 ? kInf : wk.drain[nb];
+    const double dtk = (sgn * F0) > 0. ? smin(dt, dti) : smin(dt, dtik);
+    const double c_ek = m.cek[slot];
+    const double h_ek = wk.ew[slot] - m.ze[slot];
+    const double s = dtk * sgn * c_ek;
+    r0 -= s * F0;
+    r1 -= s * F1;
+    r2 -= s * F2;
+    const double q = dt * (1. / 3.);
+    r1 -= q * wk.sx[slot] * h_ek;
+    r2 -= q * wk.sy[slot] * h_ek;
+    const double p = 0.5 * h_ek * h_ek;
+    r1 += dtk * (m.cnx[slot] * c_ek * p);
+    r2 += dtk * (m.cny[slot] * c_ek * p);
+  }
+  const double b = m.bc[i];
+  const double h0 = W0[i] - b;
+  const double c00 = h0, c01 = h0 * U0[i], c02 = h0 * V0[i];
+  double n0, n1, n2;
+  if (st.first) {
+    n0 = c00 + r0;
+    n1 = c01 + r1;
+    n2 = c02 + r2;
+  } else {
+    const double hp = Wp[i] - b;
+    const double c10 = hp, c11 = hp * Up[i], c12 = hp * Vp[i];
+    n0 = st.a * c00 + st.b * c10 + r0;
+    n1 = st.a * c01 + st.b * c11 + r1;
+    n2 = st.a * c02 + st.b * c12 + r2;
+  }
+  double ow, ou, ov;
+  cons_assign(b, n0, n1, n2, &ow, &ou, &ov);
+  Wo[i] = ow;
+  Uo[i] = ou;
+  Vo[i] = ov;
+  if (!(isfinite(ow) && isfinite(ou) && isfinite(ov))) atomicOr(wk.err, kErrNonFinite);
+}
+
+__global__ void k_init_nodes(DevMesh m, DevWork wk) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < m.N) wk.maxwp[i] = order_key(m.nz[i]);
+  if (i == 0) *wk.pwcount = 0;
+}
+
+inline int nblocks(int64_t n, int b) { return (int)((n + b - 1) / b); }
+
+}  // namespace
+
+// ------------------------------------------------------------------ engine
+template <class T>
+T* Engine::dalloc(size_t n) {
+  void* p = nullptr;
+  if (n == 0) n = 1;
+  if (cudaMalloc(&p, n * sizeof(T)) != cudaSuccess) return nullptr;
+  allocs_.push_back(p);
+  return (T*)p;
+}
+
+Engine::~Engine() {
+  for (auto& row : graphs_)
+    for (auto& g : row)
+      if (g) cudaGraphExecDestroy(g);
+  for (void* p : allocs_) cudaFree(p);
+  if (h_fixed_dt) cudaFreeHost(h_fixed_dt);
+  if (own_stream_) cudaStreamDestroy(own_stream_);
+}
+
+std::string Engine::init(std::vector<HostInstance>&& inst, int flux, int ws, int block, int* st, bool batched) {
+  *st = 0;
+  flux_ = flux;
+  ws_ = ws;
+  block_ = 256;
+  (void)block;
+  batched_ = batched;
+  const int I = (int)inst.size();
+  int64_t C = 0, E = 0, N = 0;
+  cell_off.assign(I + 1, 0);
+  edge_off.assign(I + 1, 0);
+  node_off.assign(I + 1, 0);
+  for (int q = 0; q < I; ++q) {
+    std::string err = validate_instance(inst[q]);
+    if (!err.empty()) {
+      *st = 2;
+      return (I > 1 ? "instance " + std::to_string(q) + ": " : std::string()) + err;
+    }
+    cell_off[q] = C;
+    edge_off[q] = E;
+    node_off[q] = N;
+    C += inst[q].C;
+    E += inst[q].E;
+    N += inst[q].N;
+  }
+  cell_off[I] = C;
+  edge_off[I] = E;
+  node_off[I] = N;
+  if (3 * C > (1ll << 31) - 1 || E > (1ll << 31) - 1 || N > (1ll << 31) - 1) {
+    *st = 1;
+    return "total mesh too large for int32 device indexing";
+  }
+  HostImage img;
+  img.resize((int)C, (int)E, (int)N, I);
+  for (int q = 0; q < I; ++q) precompute_instance(inst[q], q, cell_off[q], edge_off[q], node_off[q], img);
+
+  auto up = [&](auto& vec, auto*& dst) -> bool {
+    using T = typename std::remove_reference<decltype(vec)>::type::value_type;
+    T* d = dalloc<T>(vec.size());
+    if (!d) return false;
+    if (cudaMemcpy(d, vec.data(), vec.size() * sizeof(T), cudaMemcpyHostToDevice) != cudaSuccess) return false;
+    dst = d;
+    return true;
+  };
+  DevMesh& M = mesh_;
+  M.C = (int)C; M.E = (int)E; M.N = (int)N; M.I = I;
+  bool ok = true;
+  const int *p_cnode, *p_cnbr, *p_cedge, *p_cinst, *p_eown, *p_enb, *p_esl, *p_esr, *p_einst, *p_icb;
+  const unsigned char* p_cown;
+  const double *p_bc, *p_fw, *p_area, *p_zn, *p_ze, *p_cek, *p_cnx, *p_cny, *p_dry, *p_combo, *p_pw1, *p_enx, *p_eny,
+      *p_etx, *p_ety, *p_ezm, *p_elmin, *p_nz, *p_cfl, *p_cor;
+  const Pw2Rec* p_pw2;
+  ok = ok && up(img.cnode, p_cnode) && up(img.cnbr, p_cnbr) && up(img.cedge, p_cedge) && up(img.cinst, p_cinst);
+  ok = ok && up(img.cown, p_cown) && up(img.bc, p_bc) && up(img.fwthr, p_fw) && up(img.area, p_area);
+  ok = ok && up(img.zn, p_zn) && up(img.ze, p_ze) && up(img.cek, p_cek) && up(img.cnx, p_cnx) && up(img.cny, p_cny);
+  ok = ok && up(img.dry, p_dry) && up(img.combo, p_combo) && up(img.pw1, p_pw1) && up(img.pw2, p_pw2);
+  ok = ok && up(img.eown, p_eown) && up(img.enb, p_enb) && up(img.eslotl, p_esl) && up(img.eslotr, p_esr);
+  ok = ok && up(img.einst, p_einst) && up(img.enx, p_enx) && up(img.eny, p_eny) && up(img.etx, p_etx);
+  ok = ok && up(img.ety, p_ety) && up(img.ezm, p_ezm) && up(img.elmin, p_elmin) && up(img.nz, p_nz);
+  ok = ok && up(img.inst_cell_begin, p_icb) && up(img.inst_cfl, p_cfl) && up(img.inst_cor, p_cor);
+  if (!ok) {
+    *st = 6;
+    return std::string("device allocation or upload failed: ") + cudaGetErrorString(cudaGetLastError());
+  }
+  M.cnode = p_cnode; M.cnbr = p_cnbr; M.cedge = p_cedge; M.cinst = p_cinst; M.cown = p_cown;
+  M.bc = p_bc; M.fwthr = p_fw; M.area = p_area; M.zn = p_zn; M.ze = p_ze; M.cek = p_cek;
+  M.cnx = p_cnx; M.cny = p_cny; M.dry = p_dry; M.combo = p_combo; M.pw1 = p_pw1; M.pw2 = p_pw2;
+  M.eown = p_eown; M.enb = p_enb; M.eslotl = p_esl; M.eslotr = p_esr; M.einst = p_einst;
+  M.enx = p_enx; M.eny = p_eny; M.etx = p_etx; M.ety = p_ety; M.ezm = p_ezm; M.elmin = p_elmin;
+  M.nz = p_nz; M.inst_cell_begin = p_icb; M.inst_cfl = p_cfl; M.inst_cor = p_cor;
+
+  DevWork& Wk = work_;
+  Wk.ew = dalloc<double>(3 * C); Wk.eu = dalloc<double>(3 * C); Wk.ev = dalloc<double>(3 * C);
+  Wk.sx = dalloc<double>(3 * C); Wk.sy = dalloc<double>(3 * C);
+  Wk.f0 = dalloc<double>(E); Wk.f1 = dalloc<double>(E); Wk.f2 = dalloc<double>(E);
+  Wk.drain = dalloc<double>(C);
+  Wk.maxwp = dalloc<unsigned long long>(N);
+  Wk.pwlist = dalloc<int>(C);
+  Wk.pwcount = dalloc<int>(1);
+  Wk.pwrec = dalloc<double>(C);
+  Wk.r = dalloc<unsigned long long>(I);
+  Wk.dt = dalloc<double>(I);
+  Wk.tsum = dalloc<double>(I);
+  d_fixed_dt = dalloc<double>(1);
+  Wk.fixed_dt = d_fixed_dt;
+  Wk.err = dalloc<unsigned>(1);
+  for (int q = 0; q < 6; ++q) state_[q] = dalloc<double>(C);
+  d_io = dalloc<double>(3 * C);
+  if (!Wk.ew || !Wk.eu || !Wk.ev || !Wk.sx || !Wk.sy || !Wk.f0 || !Wk.f1 || !Wk.f2 || !Wk.drain || !Wk.maxwp ||
+      !Wk.pwlist || !Wk.pwcount || !Wk.pwrec || !Wk.r || !Wk.dt || !Wk.tsum || !d_fixed_dt || !Wk.err ||
+      !state_[5] || !d_io) {
+    *st = 6;
+    return "device allocation failed";
+  }
+  if (cudaMallocHost(&h_fixed_dt, sizeof(double)) != cudaSuccess) {
+    *st = 6;
+    return "pinned allocation failed";
+  }
+  cudaMemset(Wk.ew, 0, 3 * C * sizeof(double));
+  cudaMemset(Wk.eu, 0, 3 * C * sizeof(double));
+  cudaMemset(Wk.ev, 0, 3 * C * sizeof(double));
+  cudaMemset(Wk.sx, 0, 3 * C * sizeof(double));
+  cudaMemset(Wk.sy, 0, 3 * C * sizeof(double));
+  cudaMemset(Wk.f0, 0, E * sizeof(double));
+  cudaMemset(Wk.f1, 0, E * sizeof(double));
+  cudaMemset(Wk.f2, 0, E * sizeof(double));
+  cudaMemset(Wk.pwcount, 0, sizeof(int));
+  cudaMemset(Wk.dt, 0, I * sizeof(double));
+  cudaMemset(Wk.tsum, 0, I * sizeof(double));
+  cudaMemset(Wk.err, 0, sizeof(unsigned));
+  std::vector<unsigned long long> one(I, order_key(1.0));
+  cudaMemcpy(Wk.r, one.data(), I * sizeof(unsigned long long), cudaMemcpyHostToDevice);
+  if (cudaStreamCreateWithFlags(&own_stream_, cudaStreamNonBlocking) != cudaSuccess) {
+    *st = 5;
+    return "stream creation failed";
+  }
+  stream_ = own_stream_;
+  k_init_nodes<<<nblocks(N, 256), 256, 0, stream_>>>(M, Wk);
+  ++launches_;
+  cudaError_t ce = cudaStreamSynchronize(stream_);
+  if (ce != cudaSuccess) {
+    *st = 5;
+    return std::string("CUDA error during set-up: ") + cudaGetErrorString(ce);
+  }
+  host = std::move(inst);
+  return "";
+}
+
+cudaError_t Engine::reset_pass() {
+  k_init_nodes<<<nblocks(std::max(mesh_.N, 1), 256), 256, 0, stream_>>>(mesh_, work_);
+  launches_ += 1;
+  return cudaGetLastError();
+}
+
+cudaError_t Engine::interface_values(const double* W, const double* U, const double* V, int latch_mode) {
+  const int b = block_;
+  if (batched_) k_recon1<true><<<nblocks(mesh_.C, b), b, 0, stream_>>>(mesh_, work_, W, U, V, latch_mode);
+  else k_recon1<false><<<nblocks(mesh_.C, b), b, 0, stream_>>>(mesh_, work_, W, U, V, latch_mode);
+  const int g2 = std::max(1, std::min(nblocks(mesh_.C, b), 152 * 8));
+  if (batched_) k_recon2<true><<<g2, b, 0, stream_>>>(mesh_, work_, W, U, V);
+  else k_recon2<false><<<g2, b, 0, stream_>>>(mesh_, work_, W, U, V);
+  launches_ += 2;
+  return cudaGetLastError();
+}
+
+template <class FLUX>
+static void launch_flux(bool batched, int blocks, int b, cudaStream_t s, const DevMesh& m, const DevWork& w,
+                        const double* W) {
+  if (batched) k_flux<FLUX, true><<<blocks, b, 0, s>>>(m, w, W);
+  else k_flux<FLUX, false><<<blocks, b, 0, s>>>(m, w, W);
+}
+
+cudaError_t Engine::fluxes(const double* W) {
+  const int b = block_, g = nblocks(mesh_.E, b);
+  switch (flux_ * 3 + ws_) {
+    case 0: launch_flux<HLL<Rusanov>>(batched_, g, b, stream_, mesh_, work_, W); break;
+    case 1: launch_flux<HLL<Davis>>(batched_, g, b, stream_, mesh_, work_, W); break;
+    case 2: launch_flux<HLL<Einfeldt>>(batched_, g, b, stream_, mesh_, work_, W); break;
+    case 3: launch_flux<HLLC<Rusanov>>(batched_, g, b, stream_, mesh_, work_, W); break;
+    case 4: launch_flux<HLLC<Davis>>(batched_, g, b, stream_, mesh_, work_, W); break;
+    default: launch_flux<HLLC<Einfeldt>>(batched_, g, b, stream_, mesh_, work_, W); break;
+  }
+  launches_ += 1;
+  return cudaGetLastError();
+}
+
+cudaError_t Engine::launch_stage(const Stage& st, const double* const* in, const double* const* u0,
+                                 double* const* out, bool first_stage_of_step, int latch_mode, cudaEvent_t* ev) {
+  const int b = block_;
+  const int lm = first_stage_of_step ? latch_mode : 0;
+  if (ev) cudaEventRecord(ev[0], stream_);
+  if (batched_) k_recon1<true><<<nblocks(mesh_.C, b), b, 0, stream_>>>(mesh_, work_, in[0], in[1], in[2], lm);
+  else k_recon1<false><<<nblocks(mesh_.C, b), b, 0, stream_>>>(mesh_, work_, in[0], in[1], in[2], lm);
+  if (ev) cudaEventRecord(ev[1], stream_);
+  const int g2 = std::max(1, std::min(nblocks(mesh_.C, b), 152 * 8));
+  if (batched_) k_recon2<true><<<g2, b, 0, stream_>>>(mesh_, work_, in[0], in[1], in[2]);
+  else k_recon2<false><<<g2, b, 0, stream_>>>(mesh_, work_, in[0], in[1], in[2]);
+  launches_ += 2;
+  if (ev) cudaEventRecord(ev[2], stream_);
+  cudaError_t e = fluxes(in[0]);
+  if (e != cudaSuccess) return e;
+  if (ev) cudaEventRecord(ev[3], stream_);
+  k_drain<<<nblocks(std::max(mesh_.C, mesh_.N), b), b, 0, stream_>>>(mesh_, work_, in[0]);
+  if (ev) cudaEventRecord(ev[4], stream_);
+  if (batched_)
+    k_update<true><<<nblocks(mesh_.C, b), b, 0, stream_>>>(mesh_, work_, in[0], in[1], in[2], u0[0], u0[1], u0[2],
+                                                           out[0], out[1], out[2], st);
+  else
+    k_update<false><<<nblocks(mesh_.C, b), b, 0, stream_>>>(mesh_, work_, in[0], in[1], in[2], u0[0], u0[1],
+                                                            u0[2], out[0], out[1], out[2], st);
+  if (ev) cudaEventRecord(ev[5], stream_);
+  launches_ += 2;
+  return cudaGetLastError();
+}
+
+cudaError_t Engine::step_timed(int scheme, int latch_mode, double* acc) {
+  const Scheme sc = scheme_table(scheme);
+  double* S0[3] = {state(0, 0), state(0, 1), state(0, 2)};
+  double* S1[3] = {state(1, 0), state(1, 1), state(1, 2)};
+  cudaEvent_t ev[3][6];
+  for (auto& row : ev)
+    for (auto& x : row) cudaEventCreate(&x);
+  cudaError_t e = cudaSuccess;
+  for (int s = 0; s < sc.n && e == cudaSuccess; ++s) {
+    const bool last = (s == sc.n - 1);
+    const double* const* in = (s == 0) ? S0 : S1;
+    double* const* out = last ? S0 : S1;
+    e = launch_stage(sc.s[s], in, S0, out, s == 0, latch_mode, ev[s]);
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(stream_);
+  if (e == cudaSuccess) {
+    for (int s = 0; s < sc.n; ++s)
+      for (int k = 0; k < 5; ++k) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, ev[s][k], ev[s][k + 1]);
+        acc[k] += ms;
+      }
+    float tot = 0.f;
+    cudaEventElapsedTime(&tot, ev[0][0], ev[sc.n - 1][5]);
+    acc[5] += tot;
+  }
+  for (auto& row : ev)
+    for (auto& x : row) cudaEventDestroy(x);
+  return e;
+}
+
+cudaError_t Engine::step(int scheme, int latch_mode) {
+  const Scheme sc = scheme_table(scheme);
+  double* S0[3] = {state(0, 0), state(0, 1), state(0, 2)};
+  double* S1[3] = {state(1, 0), state(1, 1), state(1, 2)};
+  for (int s = 0; s < sc.n; ++s) {
+    const bool last = (s == sc.n - 1);
+    const double* const* in = (s == 0) ? S0 : S1;
+    double* const* out = last ? S0 : S1;
+    cudaError_t e = launch_stage(sc.s[s], in, S0, out, s == 0, latch_mode);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+cudaError_t Engine::run_graph(int scheme, int latch_mode, int64_t n) {
+  if (n <= 0) return cudaSuccess;
+  cudaGraphExec_t& ge = graphs_[scheme][latch_mode];
+  const int64_t per_step = launches_;
+  if (!ge) {
+    // capture on a private stream so that any caller stream (even the legacy
+    // default one) can replay the graph
+    cudaStream_t cap;
+    if (cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking) != cudaSuccess) return cudaGetLastError();
+    cudaStream_t saved = stream_;
+    stream_ = cap;
+    cudaGraph_t g;
+    cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) {
+      stream_ = saved;
+      cudaStreamDestroy(cap);
+      return e;
+    }
+    e = step(scheme, latch_mode);
+    cudaError_t e2 = cudaStreamEndCapture(cap, &g);
+    stream_ = saved;
+    cudaStreamDestroy(cap);
+    if (e != cudaSuccess) return e;
+    if (e2 != cudaSuccess) return e2;
+    e = cudaGraphInstantiate(&ge, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+      ge = nullptr;
+      return e;
+    }
+    launches_ = per_step;  // capture launched nothing
+  }
+  const int64_t kernels_per_step = 5 * scheme_table(scheme).n;
+  for (int64_t s = 0; s < n; ++s) {
+    cudaError_t e = cudaGraphLaunch(ge, stream_);
+    if (e != cudaSuccess) return e;
+  }
+  launches_ += kernels_per_step * n;
+  return cudaSuccess;
+}
+
+}  // namespace swe

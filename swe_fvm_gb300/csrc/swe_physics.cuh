@@ -1,0 +1,275 @@
+// swe_physics.cuh -- point-wise physics of the SWE_FVM step, shared by the
+// host-side geometry precompute and the sm_103a kernels.
+//
+// Every function restates one piece of the reference (NikitaMatckevich/
+// SWE_FVM) with the same operation order, so that the device results match
+// the CPU restatement bit for bit when the kernels are built without FMA
+// contraction.  g = 1 throughout (the reference is nondimensional).
+#pragma once
+
+#include <cmath>
+#include <cstdint>
+
+#if defined(__CUDACC__)
+#define SWE_HD __host__ __device__ __forceinline__
+#else
+#define SWE_HD inline
+#endif
+
+namespace swe {
+
+// include/Includes.h:30
+constexpr double kTol = 1e-13;
+// include/Bathymetry.h:5-8
+constexpr double kWetDepth = 1e-12;
+// include/Fluxes.h:28,37,73
+constexpr double kMinCapture = 1e-10;
+// include/Assigners.h:30-32
+constexpr double kEta1 = 1e-3;
+constexpr double kEta2 = 1e-6;
+constexpr double kEta4 = 1e-12;
+constexpr double kSqrt2 = 1.4142135623730951;  // std::sqrt(2), correctly rounded
+
+SWE_HD bool is_wet(double h) { return h > kWetDepth; }
+// std::min / std::max (first argument kept on ties and NaN in the second)
+SWE_HD double smin(double a, double b) { return (b < a) ? b : a; }
+SWE_HD double smax(double a, double b) { return (a < b) ? b : a; }
+
+// ---------------------------------------------------------------- geometry
+// src/PointOperations.cpp:42-48: slope (gx, gy) of the plane through three
+// points, 2x2 partial-pivot LU (pivot: first row with the largest |a_i0|).
+SWE_HD void plane_gradient(double p0x, double p0y, double p0z, double p1x, double p1y, double p1z, double p2x,
+                           double p2y, double p2z, double* gx, double* gy) {
+  double a00 = p1x - p0x, a01 = p1y - p0y, b0 = p1z - p0z;
+  double a10 = p2x - p0x, a11 = p2y - p0y, b1 = p2z - p0z;
+  if (fabs(a10) > fabs(a00)) {
+    double t;
+    t = a00; a00 = a10; a10 = t;
+    t = a01; a01 = a11; a11 = t;
+    t = b0; b0 = b1; b1 = t;
+  }
+  double l10 = a10;
+  if (a00 != 0.) l10 = a10 / a00;
+  double u11 = a11 - l10 * a01;
+  double y1 = b1 - l10 * b0;
+  double x1 = y1 / u11;
+  double x0 = (b0 - a01 * x1) / a00;
+  *gx = x0;
+  *gy = x1;
+}
+
+// (int)log2(x) for finite x > 0, truncated toward zero, from the exponent bits
+// (src/PointOperations.cpp:33).
+SWE_HD int trunc_log2(double x) {
+  int e;
+  double m = frexp(x, &e);
+  if (m == 0.5) return e - 1;
+  return (e >= 1) ? e - 1 : e;
+}
+
+// include/CubicPolyMath.h:13-15: x^3 + b x^2 + c x + d
+SWE_HD double cubic(double d, double c, double b, double x) { return x * x * x + b * x * x + c * x + d; }
+
+// src/PointOperations.cpp:26-40.  f(xmin) is carried between iterations
+// instead of re-evaluated: the same function of the same argument.
+SWE_HD double bisection(double d, double c, double b, double xmin, double xmax) {
+  double fmin_ = cubic(d, c, b, xmin);
+  double fmax_ = cubic(d, c, b, xmax);
+  if (signbit(fmin_) == signbit(fmax_)) return (fabs(fmin_) < fabs(fmax_)) ? xmin : xmax;
+  int n = 50 + trunc_log2(xmax - xmin);
+  double x = 0.;
+  bool smin_ = signbit(fmin_);
+  for (int it = 0; it <= n; it++) {
+    x = 0.5 * (xmin + xmax);
+    double fx = cubic(d, c, b, x);
+    bool sx = signbit(fx);
+    if (smin_ != sx) {
+      xmax = x;
+    } else {
+      xmin = x;
+      smin_ = sx;
+    }
+  }
+  return x;
+}
+
+// --------------------------------------------------------------- assigners
+// src/Assigners.cpp:8-20: PrimAssigner (edge writes)
+SWE_HD void prim_assign(double b, double w, double u, double v, double* ow, double* ou, double* ov) {
+  double h = w - b;
+  if (!is_wet(h)) {
+    *ow = b; *ou = 0.; *ov = 0.;
+    return;
+  }
+  if (h < kEta1) {
+    double s = kSqrt2 * h / sqrt(h * h + kEta2);
+    u *= s;
+    v *= s;
+  }
+  *ow = w; *ou = u; *ov = v;
+}
+
+// src/Assigners.cpp:28-44: ConsAssigner (cell writes)
+SWE_HD void cons_assign(double b, double h, double hu, double hv, double* ow, double* ou, double* ov) {
+  if (!is_wet(h)) {
+    *ow = b; *ou = 0.; *ov = 0.;
+    return;
+  }
+  double ih;
+  if (h < kEta1) ih = kSqrt2 * h / sqrt(h * h * h * h + kEta4);
+  else ih = 1. / h;
+  *ow = h + b;
+  *ou = hu * ih;
+  *ov = hv * ih;
+}
+
+// -------------------------------------------------------------- edge flux
+// include/SpaceDisc.h:4-18: F.n of U = (h, hu, hv), g = 1
+SWE_HD void elem_flux(double nx, double ny, double h, double hu, double hv, double* f) {
+  f[0] = 0.; f[1] = 0.; f[2] = 0.;
+  if (is_wet(h)) {
+    double hveln = hu * nx + hv * ny;
+    f[0] = hveln;
+    f[1] = (hveln / h) * hu + (0.5 * h * h) * nx;
+    f[2] = (hveln / h) * hv + (0.5 * h * h) * ny;
+  }
+}
+
+// Wave-speed plugins (src/Fluxes.cpp:5-26).  speeds() returns the pair the
+// reference's Array<2> holds.
+struct Rusanov {
+  static constexpr int id = 0;
+  SWE_HD static void speeds(double ul, double hl, double ur, double hr, double* a0, double* a1) {
+    double cl = sqrt(hl), cr = sqrt(hr);
+    double ap = smax(fabs(ul) + cl, fabs(ur) + cr);
+    *a0 = -ap;
+    *a1 = ap;
+  }
+};
+struct Davis {
+  static constexpr int id = 1;
+  SWE_HD static void speeds(double ul, double hl, double ur, double hr, double* a0, double* a1) {
+    double cl = sqrt(hl), cr = sqrt(hr);
+    *a0 = smin(ul - cl, ur - cr);
+    *a1 = smax(ul + cl, ur + cr);
+  }
+};
+struct Einfeldt {
+  static constexpr int id = 2;
+  SWE_HD static void speeds(double ul, double hl, double ur, double hr, double* a0, double* a1) {
+    double cl = sqrt(hl), cr = sqrt(hr);
+    double uRoe = (cl * ul + cl * ur) / (cl + cr);  // the reference's cl * ur
+    double cRoe = sqrt(0.5 * (hl + hr));
+    *a0 = smin(ul - cl, uRoe - cRoe);
+    *a1 = smax(ur + cr, uRoe + cRoe);
+  }
+};
+
+// Everything a flux plugin reads about one interior edge: the geometry of the
+// edge seen from its owner ("from", include/Fluxes.h:20,62-63) and the two
+// reconstructed interface states.
+struct EdgeGeom {
+  double nx, ny;  // Domain::Norm(e, from)
+  double tx, ty;  // Domain::Tang(e, from)
+  double b;       // edge-centre bathymetry
+  double lmin;    // min(2 A_from / L, 2 A_to / L)
+};
+struct SideState {
+  double w, u, v;  // interface primitive values (EdgeField slot)
+};
+
+// Fluxes::HLL<W> (include/Fluxes.h:14-54).  *lw receives the edge's
+// length-to-wavespeed ratio, or is left alone when the edge does not update it.
+template <class W>
+struct HLL {
+  static constexpr int id = 0;
+  SWE_HD static void eval(const EdgeGeom& g, const SideState& L, const SideState& R, double cor, double* lw,
+                          double* F) {
+    double ul = L.u * g.nx + L.v * g.ny;
+    double hl = L.w - g.b;
+    double ur = R.u * g.nx + R.v * g.ny;
+    double hr = R.w - g.b;
+    F[0] = 0.; F[1] = 0.; F[2] = 0.;
+    if (hl + hr <= kMinCapture) return;
+    double a0, a1;
+    W::speeds(ul, hl, ur, hr, &a0, &a1);
+    double al = smin(0., a0);
+    double ar = smax(0., a1);
+    if (ar - al <= kMinCapture) return;
+    *lw = g.lmin / (fabs(cor) + smax(-al, ar));
+    double Ul[3] = {hl, hl * L.u, hl * L.v};
+    double Ur[3] = {hr, hr * R.u, hr * R.v};
+    double Fl[3], Fr[3];
+    elem_flux(g.nx, g.ny, Ul[0], Ul[1], Ul[2], Fl);
+    elem_flux(g.nx, g.ny, Ur[0], Ur[1], Ur[2], Fr);
+#pragma unroll
+    for (int q = 0; q < 3; ++q) F[q] = (ar * Fl[q] - al * Fr[q] + (al * ar) * (Ur[q] - Ul[q])) / (ar - al);
+  }
+};
+
+// Fluxes::HLLC<W> (include/Fluxes.h:56-111)
+template <class W>
+struct HLLC {
+  static constexpr int id = 1;
+  SWE_HD static void eval(const EdgeGeom& g, const SideState& L, const SideState& R, double cor, double* lw,
+                          double* F) {
+    double ul = L.u * g.nx + L.v * g.ny;
+    double vl = L.u * g.tx + L.v * g.ty;
+    double hl = L.w - g.b;
+    double ur = R.u * g.nx + R.v * g.ny;
+    double vr = R.u * g.tx + R.v * g.ty;
+    double hr = R.w - g.b;
+    F[0] = 0.; F[1] = 0.; F[2] = 0.;
+    if (hl + hr <= kMinCapture) return;
+    double al, ar;
+    W::speeds(ul, hl, ur, hr, &al, &ar);
+    double ustar = (ar - ur) * hr * ur - (al - ul) * hl * ul + 0.5 * (hl * hl - hr * hr);
+    ustar /= (hr * (ar - ur) - hl * (al - ul));
+    *lw = g.lmin / (fabs(cor) + smax(kTol, smax(al, ar)));
+    if (ustar <= 0) {
+      double Ur[3] = {hr, hr * R.u, hr * R.v};
+      double us = vr * g.tx + ustar * g.ty;
+      double vs = vr * g.nx + ustar * g.ny;
+      double hs = hr * (ar - ur) / (ar - ustar);
+      double Us[3] = {hs, hs * us, hs * vs};
+      double Fr[3];
+      elem_flux(g.nx, g.ny, Ur[0], Ur[1], Ur[2], Fr);
+      double s = smax(0., ar);
+#pragma unroll
+      for (int q = 0; q < 3; ++q) F[q] = Fr[q] + s * (Us[q] - Ur[q]);
+    } else {
+      double Ul[3] = {hl, hl * L.u, hl * L.v};
+      double us = vl * g.tx + ustar * g.ty;
+      double vs = vl * g.nx + ustar * g.ny;
+      double hs = hl * (al - ul) / (al - ustar);
+      double Us[3] = {hs, hs * us, hs * vs};
+      double Fl[3];
+      elem_flux(g.nx, g.ny, Ul[0], Ul[1], Ul[2], Fl);
+      double s = smin(0., al);
+#pragma unroll
+      for (int q = 0; q < 3; ++q) F[q] = Fl[q] + s * (Us[q] - Ul[q]);
+    }
+  }
+};
+
+// ------------------------------------------------------- ordered doubles
+// Monotone map of doubles to unsigned 64-bit keys (for non-NaN values), so
+// that integer atomicMax / atomicMin give the exact floating-point max / min.
+SWE_HD unsigned long long order_key(double d) {
+  union {
+    double d;
+    unsigned long long u;
+  } c;
+  c.d = d;
+  return (c.u >> 63) ? ~c.u : (c.u | 0x8000000000000000ull);
+}
+SWE_HD double order_val(unsigned long long k) {
+  union {
+    double d;
+    unsigned long long u;
+  } c;
+  c.u = (k >> 63) ? (k & 0x7FFFFFFFFFFFFFFFull) : ~k;
+  return c.d;
+}
+
+}  // namespace swe

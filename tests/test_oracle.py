@@ -1,0 +1,164 @@
+"""The CPU restatement against the reference's golden data and invariants."""
+import os
+
+import numpy as np
+import pytest
+
+from oracle.oracle import JACOBI, LITERAL, Oracle
+from swe_fvm_gb300 import scenarios
+from swe_fvm_gb300.mesh import Mesh
+from tests.helpers import cons, rel_l2
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "bowl_euler.npz")
+
+
+def bowl():
+    z = np.load(GOLDEN)
+    ed = z["edges"].astype(np.int64)
+    cd = z["cells"].astype(np.int64)
+    m = Mesh(z["geometry"], ed[:, :2].copy(), ed[:, 2:].copy(), cd[:, :3].copy(), cd[:, 3:6].copy(), cd[:, 6:].copy())
+    return m, z["out0"], z["out1"]
+
+
+def test_bowl_topology_conventions():
+    """Edge k of a cell joins its nodes k and k+1, neighbour k lies across edge
+    k, and every boundary code is the solid wall -1 (notebooks/topology.dat)."""
+    m, _, _ = bowl()
+    for k in range(3):
+        e = m.cell_edges[:, k]
+        a, b = m.cell_nodes[:, k], m.cell_nodes[:, (k + 1) % 3]
+        en = m.edge_nodes[e]
+        assert np.all(((en[:, 0] == a) & (en[:, 1] == b)) | ((en[:, 0] == b) & (en[:, 1] == a)))
+        ec = m.edge_cells[e]
+        me = np.arange(m.num_cells)
+        other = np.where(ec[:, 0] == me, ec[:, 1], ec[:, 0])
+        assert np.array_equal(other, m.cell_neighbours[:, k])
+    assert set(np.unique(m.edge_cells[:, 1][m.edge_cells[:, 1] < 0])) == {-1}
+
+
+def test_bowl_initial_state_matches_driver():
+    """out0 is 1 + exp(-5 r^2) about (4, 4) at the centroids (examples/Main.cpp:182-186)."""
+    m, out0, _ = bowl()
+    prim = scenarios.gauss_wave(m)
+    assert np.max(np.abs(prim[:, 0] - out0[:, 0])) < 1e-5  # printed with 6 significant digits
+
+
+@pytest.mark.parametrize("order", [JACOBI, LITERAL])
+def test_bowl_golden_euler_step(order):
+    """One Euler step of HLL + Einfeldt, dt = 1e-3 (examples/Main.cpp:188-193).
+
+    The dump comes from an older revision of the reference, so it pins the
+    restatement only loosely: momentum increments agree to 4% (relative L2),
+    levels to 2e-4 absolute (the print precision is 1e-5)."""
+    m, out0, out1 = bowl()
+    o = Oracle(m, scenarios.gauss_wave(m), flux="HLL", wavespeed="Einfeldt", order=order)
+    o.step("Euler", 1e-3)
+    p = o.prim()
+    res = cons(p, m.centroids()[:, 2])
+    res[:, 0] = p[:, 0]
+    inc_ref = out1 - out0
+    inc = res - out0
+    assert np.max(np.abs(res[:, 0] - out1[:, 0])) < 2.5e-4
+    for c in (1, 2):
+        assert rel_l2(inc[:, c], inc_ref[:, c]) < 0.05
+
+
+def test_lake_at_rest_preserved():
+    """Still water over a stepped bed stays at rest to round-off."""
+    m, prim = scenarios.lake_at_rest(16)
+    o = Oracle(m, prim)
+    for _ in range(20):
+        o.step("SSPRK2", 5e-3)
+    p = o.prim()
+    assert np.max(np.abs(p[:, 0] - prim[:, 0])) < 1e-12
+    assert np.max(np.abs(p[:, 1:])) < 1e-12
+
+
+@pytest.mark.parametrize("scheme", ["Euler", "SSPRK2", "SSPRK3"])
+def test_positivity_and_mass(scheme):
+    """Depth never negative (exact) and volume conserved with walls."""
+    m, prim = scenarios.random_front_case(16, seed=3)
+    bc = m.centroids()[:, 2]
+    A = m.areas()
+    o = Oracle(m, prim)
+    o.compute_interface_values()
+    o.compute_fluxes()
+    vol0 = np.sum(A * (prim[:, 0] - bc))
+    for _ in range(30):
+        dt = 0.15 * o.min_len_to_wavespeed()
+        o.step(scheme, dt)
+        p = o.prim()
+        assert np.all(p[:, 0] - bc >= 0.0)
+        assert np.all(np.isfinite(p))
+    vol = np.sum(A * (p[:, 0] - bc))
+    # the dry clamp removes at most 1e-12 of depth per cell and update
+    assert abs(vol - vol0) <= 1e-12 * m.num_cells * 30 * A.max() + 1e-13 * abs(vol0)
+
+
+def test_reconstruction_branches_present():
+    """The front case exercises dry, partially-wet and fully-wet cells."""
+    m, prim = scenarios.random_front_case(20, seed=1)
+    o = Oracle(m, prim)
+    cls = o.classify()
+    assert set(np.unique(cls)) == {0, 1, 2}
+
+
+def test_jacobi_conserves_mass_literal_order_does_not():
+    """The reference's in-place update (RHS reads neighbours that this stage has
+    already overwritten, src/Solvers.cpp:23-25 with src/TimeDisc.cpp:25,47,64)
+    makes the two sides of an edge use different draining time steps, so
+    volume leaks; the order-independent (jacobi) reading conserves it."""
+    m, prim = scenarios.thacker(16, quad=10)
+    bc, A = m.centroids()[:, 2], m.areas()
+    a = Oracle(m, prim, order=JACOBI)
+    b = Oracle(m, prim, order=LITERAL)
+    vol0 = np.sum(A * (prim[:, 0] - bc))
+    for _ in range(5):
+        a.step("SSPRK2", 0.01)
+        b.step("SSPRK2", 0.01)
+    va = np.sum(A * (a.prim()[:, 0] - bc))
+    vb = np.sum(A * (b.prim()[:, 0] - bc))
+    assert abs(va - vol0) < 1e-13 * vol0
+    assert abs(vb - vol0) > 1e-6 * vol0
+
+
+def test_thacker_tracks_the_analytic_solution():
+    """Sanity: the depth error against the closed form (examples/Tests.h:237-280)
+    after t = 0.4 is small and shrinks under refinement."""
+    errs = []
+    for n in (16, 32):
+        m, prim = scenarios.thacker(n, quad=10)
+        o = Oracle(m, prim)
+        for _ in range(80):
+            o.step("SSPRK2", 0.005)
+        _, ana = scenarios.thacker(n, quad=10, t=0.4)
+        bc = m.centroids()[:, 2]
+        errs.append(rel_l2(o.prim()[:, 0] - bc, ana[:, 0] - bc))
+    assert errs[0] < 0.1 and errs[1] < 0.8 * errs[0]
+
+
+def test_unit_functions():
+    """Known answers of the point-wise pieces."""
+    from oracle import oracle as O
+    import ctypes
+
+    L = O.lib()
+    a = np.zeros(2)
+    L.oracle_wavespeed(2, 0.1, 1.0, -0.1, 0.5, a.ctypes.data_as(ctypes.c_void_p))
+    cl, cr = 1.0, np.sqrt(0.5)
+    uroe = (cl * 0.1 + cl * -0.1) / (cl + cr)
+    croe = np.sqrt(0.75)
+    assert a[0] == min(0.1 - cl, uroe - croe) and a[1] == max(-0.1 + cr, uroe + croe)
+    # bisection of x^3 - 2 on [1, 2] converges to 2^(1/3)
+    r = L.oracle_bisection_cubic(-2.0, 0.0, 0.0, 1.0, 2.0)
+    assert abs(r - 2 ** (1 / 3)) < 1e-14
+    # plane through (0,0,0), (1,0,2), (0,1,3) has slope (2, 3)
+    p0, p1, p2, g = np.array([0., 0, 0]), np.array([1., 0, 2]), np.array([0., 1, 3]), np.zeros(2)
+    vp = lambda x: x.ctypes.data_as(ctypes.c_void_p)
+    L.oracle_gradient3(vp(p0), vp(p1), vp(p2), vp(g))
+    assert np.allclose(g, [2, 3], atol=0, rtol=1e-15)
+    out = np.zeros(3)
+    L.oracle_cons_assign(1.0, vp(np.array([1e-13, 1., 1.])), vp(out))
+    assert list(out) == [1.0, 0.0, 0.0]
+    L.oracle_prim_assign(1.0, vp(np.array([1.5, 2., 3.])), vp(out))
+    assert list(out) == [1.5, 2.0, 3.0]
