@@ -224,8 +224,8 @@ __global__ void __launch_bounds__(256) k_recon1(DevMesh m, DevWork wk, const dou
 template <bool BATCH>
 __global__ void __launch_bounds__(256) k_recon2(DevMesh m, DevWork wk, const double* __restrict__ W,
                                                 const double* __restrict__ U, const double* __restrict__ V) {
-  const int n = *wk.pwcount;
   const int C = m.C;
+  const int n = min(*wk.pwcount, C);
   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
     const int i = wk.pwlist[q];
     const int inst = BATCH ? m.cinst[i] : 0;
