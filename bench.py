@@ -20,6 +20,7 @@ of the reference solver on the host cores instead.
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
 import os
 import statistics
@@ -201,13 +202,15 @@ def run_gpu(args):
            "d2h_bytes_per_step": 24 * C, "steps": n_e2e,
            "api": "swe_set_prim + swe_step + swe_get_prim (pinned host buffers)"}
 
+    fp64 = ctypes.c_double(0.0)
+    _lib.check(L.swe_measure_fp64_peak(ctypes.byref(fp64)))
     hbm, src = peaks()
     achieved = BYTES_PER_CELL_STEP * C / (ms_step * 1e-3) / 1e9
     roof = {"bound": "hbm", "kernel": "ssprk2_step (2 stages x 5 kernels, one CUDA graph)", "achieved": achieved,
             "peak": hbm, "unit": "GB/s", "frac": achieved / hbm, "peak_source": src,
             "algorithmic_bytes_per_launch": BYTES_PER_CELL_STEP * C,
             "traffic": TRAFFIC_PER_STEP.get(LATTICE),
-            "kernel_ms_per_launch": per}
+            "kernel_ms_per_launch": per, "fp64_peak_tflops_measured": fp64.value}
 
     out = {
         "metric": "cell-updates/s (plain FP64 SSPRK2 step, 1M-triangle unstructured mesh)",

@@ -147,6 +147,11 @@ swe_status swe_get_node_max(swe_ctx* ctx, double* max_out);
  * time.  Advances the state; synchronises.  No reference counterpart. */
 swe_status swe_time_kernels(swe_ctx* ctx, int32_t scheme, int64_t reps, double* out_ms);
 
+/* FP64 FMA throughput of the current device in TFLOP/s (best of 5 timed
+ * launches of independent FMA chains): the arithmetic ceiling of the step.
+ * No reference counterpart. */
+swe_status swe_measure_fp64_peak(double* tflops);
+
 /* Size and counters. */
 swe_status swe_num_cells(swe_ctx* ctx, int64_t* n);
 /* Kernel launches issued so far by this context (all streams, graphs counted
