@@ -150,7 +150,9 @@ def run_gpu(args):
     mesh, prim, t_gen = workload()
     C = mesh.num_cells
     sd = SpaceDisc(Fluxes.HLLC(Wavespeeds.Einfeldt), mesh, prim, cfl=CFL)
-    stream = torch.cuda.current_stream()
+    # a dedicated stream: the library's kernels and the timing events share it
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     sd.set_stream(stream.cuda_stream)
     # warm-up (graph capture happens on the first replay)
     sd.run_cfl(1, args.warmup)

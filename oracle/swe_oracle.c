@@ -835,12 +835,13 @@ void oracle_get_prim(const oracle_ctx* c, double* out) {
 void oracle_set_prim(oracle_ctx* c, const double* in) {
   memcpy(c->vol, in, (size_t)c->m.num_cells * 3 * sizeof(double));
 }
-/* edge fields in the reference layout: 3 x 2E each; fluxes 3 x E; node maxima N */
+/* edge fields in the reference layout: 3 x 2E each; fluxes 3 x E; node maxima
+ * N as pass 2 reads them (jacobi: after pass 1; literal: the live array) */
 void oracle_get_edge_fields(const oracle_ctx* c, double* edg, double* src, double* f, double* max_wp) {
   if (edg) memcpy(edg, c->edg, (size_t)c->m.num_edges * 6 * sizeof(double));
   if (src) memcpy(src, c->src, (size_t)c->m.num_edges * 6 * sizeof(double));
   if (f) memcpy(f, c->f, (size_t)c->m.num_edges * 3 * sizeof(double));
-  if (max_wp) memcpy(max_wp, c->max_wp, (size_t)c->m.num_nodes * sizeof(double));
+  if (max_wp) memcpy(max_wp, c->maxwp_read, (size_t)c->m.num_nodes * sizeof(double));
 }
 
 /* Per-cell class as the reconstruction pass 1 sees it: 0 dry, 1 part-wet, 2 full-wet */
