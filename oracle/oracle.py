@@ -61,6 +61,8 @@ def lib():
         L.oracle_gradient3.argtypes = [vp, vp, vp, vp]
         L.oracle_prim_assign.argtypes = [d, vp, vp]
         L.oracle_cons_assign.argtypes = [d, vp, vp]
+        L.oracle_cbrt_rn.argtypes = [d]
+        L.oracle_cbrt_rn.restype = d
         _lib = L
     return _lib
 

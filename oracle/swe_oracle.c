@@ -25,6 +25,10 @@
  *     stage come from the start-of-stage state and pass 2 of the reconstruction
  *     read the pass-1 node maxima only.  JACOBI is the GPU parity target.
  *   - Eigen 3.4's 2x2 partialPivLu solve is restated with the same pivot rule.
+ *   - std::cbrt (src/MUSCLObject.cpp:103) is replaced by the correctly rounded
+ *     cube root (libm cube roots are faithful only and disagree in the last
+ *     bit across libraries).
+ *   - (int)log2(b - a) in Bisection is taken exactly from the binary exponent.
  *
  * Build: -O2 -ffp-contract=off (no FMA contraction, so results do not depend on
  * whether the host compiler fuses multiply-adds).
@@ -295,6 +299,59 @@ static muscl_t ReconstructDryCell(const oracle_ctx* c, int64_t i) {
   return m;
 }
 
+/* Correctly rounded cube root (nearest, ties to even).  std::cbrt is only
+ * faithful and its last bit differs between math libraries, so the level of
+ * src/MUSCLObject.cpp:103 is restated with the exactly rounded value:
+ * x = Mx 2^E (Mx a 53-bit integer), N = Mx 2^t with t in {107,108,109},
+ * 3 | (E - t); Y = floor(cbrt(N)) in [2^53, 2^54) from a libm estimate
+ * corrected by exact 192-bit cubes; Y's last bit and N - Y^3 round it. */
+typedef unsigned __int128 u128;
+typedef struct { uint64_t w[3]; } u192;
+static u192 cube192(uint64_t y) {
+  u128 y2 = (u128)y * y;
+  u128 lo = (u128)(uint64_t)y2 * y;
+  u128 hi = (u128)(uint64_t)(y2 >> 64) * y;
+  u192 r;
+  r.w[0] = (uint64_t)lo;
+  u128 mid = (lo >> 64) + (uint64_t)hi;
+  r.w[1] = (uint64_t)mid;
+  r.w[2] = (uint64_t)((mid >> 64) + (hi >> 64));
+  return r;
+}
+static int cmp192(u192 a, u192 b) {
+  for (int k = 2; k >= 0; --k) {
+    if (a.w[k] != b.w[k]) return a.w[k] < b.w[k] ? -1 : 1;
+  }
+  return 0;
+}
+double oracle_cbrt_rn(double x) {
+  if (x != x || x == 0. || isinf(x)) return x + x;
+  int neg = x < 0.;
+  double ax = neg ? -x : x;
+  int scale = 0;
+  if (ax < 2.2250738585072014e-308) { ax *= 18014398509481984.0; scale = -18; }
+  int e;
+  double m = frexp(ax, &e);
+  uint64_t Mx = (uint64_t)ldexp(m, 53);
+  int E = e - 53;
+  int t = 107;
+  while (((E - t) % 3 + 3) % 3 != 0) ++t;
+  u192 N = {{0, 0, 0}};
+  N.w[t / 64] = Mx << (t % 64);
+  if (t % 64) N.w[t / 64 + 1] = Mx >> (64 - t % 64);
+  double est = ldexp(cbrt((double)Mx * ldexp(1.0, t % 3)), t / 3);
+  uint64_t Y = (uint64_t)est;
+  if (Y < (1ull << 53)) Y = 1ull << 53;
+  if (Y >= (1ull << 54)) Y = (1ull << 54) - 1;
+  for (int it = 0; it < 64 && cmp192(cube192(Y), N) > 0; ++it) --Y;
+  for (int it = 0; it < 64 && cmp192(cube192(Y + 1), N) <= 0; ++it) ++Y;
+  int sticky = cmp192(cube192(Y), N) != 0;
+  uint64_t R = Y >> 1;
+  if ((Y & 1u) && (sticky || (R & 1u))) ++R;
+  double r = ldexp((double)R, (E - t) / 3 + 1 + scale);
+  return neg ? -r : r;
+}
+
 /* src/PointOperations.cpp:26-40 on the cubic of include/CubicPolyMath.h:13-15
  * (coefficients in the reference's constructor order d, c, b). */
 static double cubic(double d, double cc, double b, double x) { return x * x * x + b * x * x + cc * x + d; }
@@ -336,7 +393,7 @@ static muscl_t ReconstructPartWetCell1(const oracle_ctx* c, int64_t i) {
   if (w >= b13) {
     w_rec = w;
   } else if (w <= b_delim) {
-    w_rec = b23 + cbrt(3. * h * (b13 - b23) * (b12 - b23));
+    w_rec = b23 + oracle_cbrt_rn(3. * h * (b13 - b23) * (b12 - b23));
   } else {
     double a = -3. * b13;
     double bb = 3. * (b12 * b13 + b13 * b23 - b12 * b23);

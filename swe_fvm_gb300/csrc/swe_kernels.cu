@@ -89,7 +89,7 @@ __device__ __forceinline__ void node_max(const DevWork& wk, int node, double val
 __device__ __forceinline__ double partwet1_level(const double* __restrict__ p, double w, double h) {
   const double b13 = p[0], b23 = p[1], b12 = p[2], bdel = p[3];
   if (w >= b13) return w;
-  if (w <= bdel) return b23 + cbrt(3. * h * p[6] * p[7]);
+  if (w <= bdel) return b23 + cbrt_rn(3. * h * p[6] * p[7]);
   double cc = p[6] * (3. * h * p[8] - p[9]) - p[10];
   (void)b12;
   return bisection(cc, p[5], p[4], p[2], b13);

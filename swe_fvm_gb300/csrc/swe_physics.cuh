@@ -67,6 +67,73 @@ SWE_HD int trunc_log2(double x) {
   return (e >= 1) ? e - 1 : e;
 }
 
+// Correctly rounded cube root (round to nearest, ties to even) for the
+// PartWet1 level (src/MUSCLObject.cpp:103).  The math libraries' cbrt are
+// faithful, not correctly rounded, and the CUDA and host ones differ in the
+// last bit; this one is exact on both.  Method: x = Mx 2^E with a 53-bit
+// integer Mx; N = Mx 2^t with t in {107, 108, 109} chosen so that 3 | (E - t)
+// and N in [2^159, 2^162); Y = floor(cbrt(N)) in [2^53, 2^54) is found from a
+// library estimate corrected with exact 192-bit integer cubes; its lowest bit
+// and the remainder N - Y^3 round it to 53 bits.
+struct U192 {
+  unsigned long long w[3];  // little-endian limbs
+};
+SWE_HD U192 u192_cube(unsigned long long y) {
+  // y < 2^55: y^2 < 2^110 fits 128 bits, y^3 < 2^165 fits 192 bits
+  unsigned __int128 y2 = (unsigned __int128)y * y;
+  unsigned __int128 lo = (unsigned __int128)(unsigned long long)y2 * y;
+  unsigned __int128 hi = (unsigned __int128)(unsigned long long)(y2 >> 64) * y;
+  U192 r;
+  r.w[0] = (unsigned long long)lo;
+  unsigned __int128 mid = (lo >> 64) + (unsigned long long)hi;
+  r.w[1] = (unsigned long long)mid;
+  r.w[2] = (unsigned long long)((mid >> 64) + (hi >> 64));
+  return r;
+}
+SWE_HD int u192_cmp(const U192& a, const U192& b) {
+  for (int k = 2; k >= 0; --k) {
+    if (a.w[k] < b.w[k]) return -1;
+    if (a.w[k] > b.w[k]) return 1;
+  }
+  return 0;
+}
+SWE_HD double cbrt_rn(double x) {
+  if (!(x == x) || x == 0. || isinf(x)) return x + x;  // NaN, +-0, +-inf
+  const bool neg = x < 0.;
+  double ax = neg ? -x : x;
+  int scale = 0;
+  if (ax < 2.2250738585072014e-308) {  // subnormal: scale by 2^54
+    ax = ax * 18014398509481984.0;
+    scale = -18;
+  }
+  int e;
+  const double m = frexp(ax, &e);                                  // ax = m 2^e, m in [0.5, 1)
+  const unsigned long long Mx = (unsigned long long)ldexp(m, 53);  // exact 53-bit integer
+  const int E = e - 53;                                            // ax = Mx 2^E
+  int t = 107;
+  while (((E - t) % 3 + 3) % 3 != 0) ++t;
+  // N = Mx 2^t as 192 bits
+  U192 N;
+  {
+    const int word = t / 64, bit = t % 64;
+    N.w[0] = N.w[1] = N.w[2] = 0ull;
+    N.w[word] = Mx << bit;
+    if (bit && word + 1 < 3) N.w[word + 1] = Mx >> (64 - bit);
+  }
+  // estimate: cbrt(Mx 2^t) = cbrt(Mx) 2^(t/3)
+  const double est = ldexp(cbrt((double)Mx * ldexp(1.0, t % 3)), t / 3);
+  unsigned long long Y = (unsigned long long)est;
+  if (Y < (1ull << 53)) Y = 1ull << 53;
+  if (Y >= (1ull << 54)) Y = (1ull << 54) - 1;
+  for (int it = 0; it < 64 && u192_cmp(u192_cube(Y), N) > 0; ++it) --Y;
+  for (int it = 0; it < 64 && u192_cmp(u192_cube(Y + 1), N) <= 0; ++it) ++Y;
+  const bool sticky = u192_cmp(u192_cube(Y), N) != 0;
+  unsigned long long R = Y >> 1;
+  if ((Y & 1ull) && (sticky || (R & 1ull))) ++R;
+  const double r = ldexp((double)R, (E - t) / 3 + 1 + scale);
+  return neg ? -r : r;
+}
+
 // include/CubicPolyMath.h:13-15: x^3 + b x^2 + c x + d
 SWE_HD double cubic(double d, double c, double b, double x) { return x * x * x + b * x * x + c * x + d; }
 

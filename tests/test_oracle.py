@@ -162,3 +162,24 @@ def test_unit_functions():
     assert list(out) == [1.0, 0.0, 0.0]
     L.oracle_prim_assign(1.0, vp(np.array([1.5, 2., 3.])), vp(out))
     assert list(out) == [1.5, 2.0, 3.0]
+
+
+def test_cbrt_correctly_rounded():
+    """The cube root used by PartWet1 is the nearest double to the exact root
+    (checked with exact rational arithmetic), ties to even."""
+    from fractions import Fraction
+
+    from oracle import oracle as O
+
+    L = O.lib()
+    rng = np.random.default_rng(0)
+    xs = list(np.exp(rng.uniform(-60, 60, 3000))) + [1.0, 8.0, 27.0, 2.0, 3.0, 1e-300, 5e-324, 1e300, 0.125]
+    for x in xs:
+        y = L.oracle_cbrt_rn(float(x))
+        fx = Fraction(float(x))
+        fy = Fraction(y)
+        lo = Fraction(np.nextafter(y, 0.0))
+        hi = Fraction(np.nextafter(y, np.inf))
+        # y is nearest: (y+lo)/2 <= cbrt(x) <= (y+hi)/2, compared by cubing
+        assert ((fy + lo) / 2) ** 3 <= fx <= ((fy + hi) / 2) ** 3, x
+    assert L.oracle_cbrt_rn(-8.0) == -2.0 and L.oracle_cbrt_rn(0.0) == 0.0
