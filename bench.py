@@ -154,6 +154,13 @@ def run_gpu(args):
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
     sd.set_stream(stream.cuda_stream)
+    if args.profile:
+        # profiling driver: warm-up, then exactly K graph-replayed steps
+        sd.run_cfl(1, args.warmup)
+        sd.run_cfl(1, args.steps)
+        sd.synchronize()
+        print(json.dumps({"profile": True, "cells": C, "steps": args.steps, "warmup": args.warmup}))
+        return
     # warm-up (graph capture happens on the first replay)
     sd.run_cfl(1, args.warmup)
     torch.cuda.synchronize()
@@ -282,6 +289,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--profile", action="store_true", help="only warm-up + K steps (for ncu captures)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
