@@ -164,6 +164,29 @@ swe_status swe_synchronize(swe_ctx* ctx);
  * on this thread).  Never NULL. */
 const char* swe_last_error(swe_ctx* ctx);
 
+/* Edge-flux pass that allocates no device memory, for callers that cannot call
+ * cudaMalloc (a framework owning all device memory through its own pool, a
+ * real-time loop that forbids allocation, a plugin handed only device
+ * pointers).  No counterpart in the reference.
+ *
+ * For n_edges interior edges it evaluates the flux plugin (flux x wavespeed)
+ * exactly as one edge of SpaceDisc::ComputeFluxes does, and the minimum
+ * length-to-wavespeed ratio, reset to 1 first.  All pointers are device
+ * memory: edge_geom 6 x n_edges column-major (nx, ny, tx, ty, b, lmin per edge:
+ * the owner's outward normal and tangent, edge-centre bathymetry and
+ * min(2 A_owner / L, 2 A_neighbour / L)); left / right 3 x n_edges interface
+ * primitives (w, u, v) of the owner and the neighbour; flux_out 3 x n_edges;
+ * ratio_out one double.  Asynchronous on `stream` (NULL = legacy default).
+ *
+ * Scratch lives in a static 512 KB device array held by every GPU that loads
+ * this library, so n_edges is limited to 16,777,216 (larger requests return
+ * SWE_ERR_INVALID_ARGUMENT).  The first call on a device looks up that array's
+ * device address (make it before any stream capture).  All calls share the
+ * array: calls that overlap on the GPU (other streams, other threads) race. */
+swe_status swe_edge_fluxes_noalloc(int32_t flux, int32_t wavespeed, int64_t n_edges, const double* edge_geom,
+                                   const double* left, const double* right, double cor, double* flux_out,
+                                   double* ratio_out, void* stream);
+
 /* ---------------------------------------------------------------- batched */
 /* Many independent instances (each its own mesh, state, parameters and CFL
  * step) stepped together: cells and edges of all instances are concatenated
