@@ -232,12 +232,74 @@ def run_gpu(args):
                    "parallelism": f"replicas x{world}", "mesh_gen_s": round(t_gen, 1)},
         "e2e": e2e, "gpu_launches": launches, "roofline": roof, "clocks": clk.summary(),
     }
+    if ENSEMBLE_INSTANCES > 0 and not args.no_ensemble:
+        out["batched"] = run_ensemble(torch, stream)
     if rank == 0:
         if world == 1 and not args.no_cpu:
             out["cpu_baseline"] = cpu_baseline(mesh, prim)
         print(json.dumps(out), flush=True)
     if dist:
         dist.destroy_process_group()
+
+
+ENSEMBLE_INSTANCES = int(os.environ.get("SWE_BENCH_ENSEMBLE", "256"))
+ENSEMBLE_STEPS = int(os.environ.get("SWE_BENCH_ENSEMBLE_STEPS", "200"))
+
+
+def run_ensemble(torch, stream):
+    """Ensemble config: 256 seeded Delaunay instances, 2k-200k cells
+    (log-uniform), HLLC + Einfeldt, SSPRK2, per-instance CFL 0.4, 200 steps.
+    Batched: every stage kernel covers all instances (one graph per step).
+    Plain: the same instances stepped one after another with the plain step."""
+    from swe_fvm_gb300 import Batch, Fluxes, SpaceDisc, Wavespeeds, scenarios
+
+    t0 = time.time()
+    ens = scenarios.ensemble(ENSEMBLE_INSTANCES)
+    t_gen = time.time() - t0
+    meshes = [m for m, _ in ens]
+    prims = [p for _, p in ens]
+    cells = sum(m.num_cells for m in meshes)
+    fl = Fluxes.HLLC(Wavespeeds.Einfeldt)
+    K = ENSEMBLE_STEPS
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    # batched
+    b = Batch(meshes, prims, fl, cfl=0.4)
+    b.set_stream(stream.cuda_stream)
+    b.run_cfl(1, 3)
+    torch.cuda.synchronize()
+    n0 = b.launch_count()
+    e0.record(stream)
+    b.run_cfl(1, K)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms_b = e0.elapsed_time(e1)
+    launches_b = b.launch_count() - n0
+    b.synchronize()
+    del b
+    # plain, one instance after another
+    sds = []
+    for m, p in ens:
+        sd = SpaceDisc(fl, m, p, cfl=0.4)
+        sd.set_stream(stream.cuda_stream)
+        sd.run_cfl(1, 3)
+        sds.append(sd)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for sd in sds:
+        sd.run_cfl(1, K)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms_p = e0.elapsed_time(e1)
+    for sd in sds:
+        sd.synchronize()
+    del sds
+    vb = cells * K / (ms_b * 1e-3)
+    vp = cells * K / (ms_p * 1e-3)
+    return {"metric": "cell-updates/s (batched FP64 SSPRK2 ensemble)", "value": vb, "unit": "cell-updates/s",
+            "plain_sequential_value": vp, "speedup_vs_plain": vb / vp, "instances": len(ens), "cells": cells,
+            "steps": K, "ms_per_step": ms_b / K, "plain_ms_per_step": ms_p / K, "gpu_launches": launches_b,
+            "config": {"workload": "ensemble_256", "cells_per_instance": "log-uniform 2k-200k", "cfl": 0.4,
+                       "flux": "HLLC+Einfeldt", "scheme": "SSPRK2", "mesh_gen_s": round(t_gen, 1)}}
 
 
 # DRAM bytes per SSPRK2 step from the ncu launch capture (sum over the step's
@@ -290,6 +352,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--profile", action="store_true", help="only warm-up + K steps (for ncu captures)")
+    ap.add_argument("--no-ensemble", action="store_true", help="skip the batched-ensemble leg")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

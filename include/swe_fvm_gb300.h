@@ -195,6 +195,8 @@ swe_status swe_edge_fluxes_noalloc(int32_t flux, int32_t wavespeed, int64_t n_ed
 swe_status swe_batch_create(int32_t n_instances, const swe_mesh* meshes, const double* const* prim0,
                             const swe_params* params, int32_t n_params, swe_batch** out);
 swe_status swe_batch_destroy(swe_batch* b);
+/* Runs the batch's kernels on `stream` (NULL = the batch's own stream). */
+swe_status swe_batch_set_stream(swe_batch* b, void* stream);
 /* n_steps steps of every instance, each with its own dt = cfl * ratio taken
  * before every step; one CUDA graph per step replayed n_steps times. */
 swe_status swe_batch_run_cfl(swe_batch* b, int32_t scheme, int64_t n_steps);

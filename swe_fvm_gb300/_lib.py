@@ -30,7 +30,7 @@ EXPORTS = [
     "swe_cfl_dt", "swe_min_len_to_wavespeed", "swe_compute_interface_values", "swe_compute_fluxes",
     "swe_get_prim", "swe_set_prim", "swe_get_prim_device", "swe_set_prim_device", "swe_get_edge_values",
     "swe_get_fluxes", "swe_get_node_max", "swe_time_kernels", "swe_measure_fp64_peak", "swe_num_cells", "swe_launch_count", "swe_synchronize",
-    "swe_last_error", "swe_edge_fluxes_noalloc", "swe_batch_create", "swe_batch_destroy", "swe_batch_run_cfl", "swe_batch_run",
+    "swe_last_error", "swe_edge_fluxes_noalloc", "swe_batch_create", "swe_batch_destroy", "swe_batch_set_stream", "swe_batch_run_cfl", "swe_batch_run",
     "swe_batch_get_prim", "swe_batch_time", "swe_batch_launch_count", "swe_batch_synchronize",
     "swe_batch_last_error",
 ]
@@ -113,6 +113,7 @@ def load(build_if_needed: bool = True):
         "swe_edge_fluxes_noalloc": [i32, i32, i64, vp, vp, vp, d, vp, vp, vp],
         "swe_batch_create": [i32, vp, vp, P(SweParams), i32, P(vp)],
         "swe_batch_destroy": [vp],
+        "swe_batch_set_stream": [vp, vp],
         "swe_batch_run_cfl": [vp, i32, i64],
         "swe_batch_run": [vp, i32, d, i64],
         "swe_batch_get_prim": [vp, i32, vp],

@@ -496,6 +496,12 @@ swe_status swe_batch_destroy(swe_batch* b) {
   return SWE_OK;
 }
 
+swe_status swe_batch_set_stream(swe_batch* b, void* stream) {
+  if (!b) return SWE_ERR_INVALID_ARGUMENT;
+  b->eng.set_stream(stream ? (cudaStream_t)stream : nullptr);
+  return SWE_OK;
+}
+
 swe_status swe_batch_run_cfl(swe_batch* b, int32_t scheme, int64_t n_steps) {
   if (!b) return SWE_ERR_INVALID_ARGUMENT;
   if (scheme < 0 || scheme > 2 || n_steps < 0) return fail(&b->err, SWE_ERR_INVALID_ARGUMENT, "bad scheme or n_steps");

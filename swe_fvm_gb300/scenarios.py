@@ -148,6 +148,27 @@ def ensemble_sizes(n_instances: int = 256, lo: int = 2000, hi: int = 200000, see
     return np.exp(rng.uniform(math.log(lo), math.log(hi), n_instances)).astype(np.int64)
 
 
+def _hump_job(args):
+    seed, cells = args
+    return hump_instance(seed, cells)
+
+
+def ensemble(n_instances: int = 256, lo: int = 2000, hi: int = 200000, seed0: int = 1000, processes: int = 0):
+    """Config: n_instances seeded instances (instance i uses seed seed0 + i) with
+    cell counts log-uniform in [lo, hi].  Generated in `spawn` worker processes
+    (safe to call before or after CUDA is initialised in the parent)."""
+    import multiprocessing as mp
+    import os
+
+    sizes = ensemble_sizes(n_instances, lo, hi)
+    jobs = [(seed0 + i, int(c)) for i, c in enumerate(sizes)]
+    nproc = processes or max(1, min(16, (os.cpu_count() or 1)))
+    if nproc == 1:
+        return [_hump_job(j) for j in jobs]
+    with mp.get_context("spawn").Pool(nproc) as pool:
+        return pool.map(_hump_job, jobs, chunksize=1)
+
+
 # ---------------------------------------------------------------- small cases
 def lake_at_rest(n: int = 32, level: float = 0.0):
     """Still water over a stepped bed on [0,4]^2 (examples/Tests.h:37-42): bed

@@ -346,6 +346,9 @@ class Batch:
     def run_cfl(self, scheme: int, n_steps: int) -> None:
         self._check(_lib.load().swe_batch_run_cfl(self.b, int(scheme), int(n_steps)))
 
+    def set_stream(self, stream_ptr: int) -> None:
+        self._check(_lib.load().swe_batch_set_stream(self.b, ctypes.c_void_p(stream_ptr)))
+
     def run(self, scheme: int, dt: float, n_steps: int) -> None:
         self._check(_lib.load().swe_batch_run(self.b, int(scheme), float(dt), int(n_steps)))
 
