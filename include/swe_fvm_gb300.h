@@ -152,6 +152,13 @@ swe_status swe_time_kernels(swe_ctx* ctx, int32_t scheme, int64_t reps, double* 
  * No reference counterpart. */
 swe_status swe_measure_fp64_peak(double* tflops);
 
+/* Compares the integer-pipe FP64 division and square root used by the kernels
+ * with the hardware instructions on n pseudo-random operands (all classes:
+ * normal, near-power-of-two significands, extreme exponents, specials) and
+ * returns the number of results that differ in any bit.  No reference
+ * counterpart. */
+swe_status swe_selftest_fp64(int64_t n, uint64_t seed, int64_t* div_mismatches, int64_t* sqrt_mismatches);
+
 /* Size and counters. */
 swe_status swe_num_cells(swe_ctx* ctx, int64_t* n);
 /* Kernel launches issued so far by this context (all streams, graphs counted

@@ -54,3 +54,75 @@ extern "C" swe_status swe_measure_fp64_peak(double* tflops) {
   *tflops = flops / (best * 1e-3) / 1e12;
   return SWE_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Self-test of the integer-pipe division and square root (swe_fp64.cuh)
+// against the hardware instructions on n pseudo-random operand pairs.
+
+#include "swe_fp64.cuh"
+
+namespace {
+
+__device__ __forceinline__ unsigned long long splitmix(unsigned long long z) {
+  z += 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+// operand classes: random bits anywhere; exponents near 1; significands near
+// 1 (tiny fraction) or near 2 (all ones); random bits with the full exponent range
+__device__ double make_operand(unsigned long long r, unsigned long long r2) {
+  const unsigned mode = (unsigned)(r2 & 7u);
+  unsigned long long sign = (r2 >> 8) & 1ull;
+  unsigned long long exp, man = r & ((1ull << 52) - 1ull);
+  switch (mode) {
+    case 0: return __longlong_as_double((long long)r);  // anything, specials included
+    case 1: exp = 1023 - 40 + ((r2 >> 16) % 81); break;
+    case 2: exp = 1023 - 40 + ((r2 >> 16) % 81); man &= 0xFFFull; break;                       // 1 + tiny
+    case 3: exp = 1023 - 40 + ((r2 >> 16) % 81); man |= ((1ull << 52) - 1ull) ^ 0xFFFull; break;  // near 2
+    case 4: exp = 1 + ((r2 >> 16) % 2046); break;                                               // full normal range
+    case 5: exp = 1 + ((r2 >> 16) % 60); break;                                                 // near underflow
+    case 6: exp = 2046 - ((r2 >> 16) % 60); break;                                              // near overflow
+    default: exp = 1023 + ((r2 >> 16) % 5) - 2; man = (r2 >> 20) & ((1ull << 52) - 1ull); break;
+  }
+  return __longlong_as_double((long long)((sign << 63) | (exp << 52) | man));
+}
+
+__global__ void k_fp64_selftest(long long n, unsigned long long seed, unsigned long long* counts) {
+  unsigned long long bad_div = 0, bad_sqrt = 0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const unsigned long long r0 = splitmix(seed ^ (4ull * i)), r1 = splitmix(seed ^ (4ull * i + 1));
+    const unsigned long long r2 = splitmix(seed ^ (4ull * i + 2)), r3 = splitmix(seed ^ (4ull * i + 3));
+    const double a = make_operand(r0, r1), b = make_operand(r2, r3);
+    const double q_soft = swe::ddiv_rn(a, b), q_hw = __ddiv_rn(a, b);
+    const bool nan_both = (q_soft != q_soft) && (q_hw != q_hw);
+    if (!nan_both && __double_as_longlong(q_soft) != __double_as_longlong(q_hw)) ++bad_div;
+    const double x = fabs(a);
+    const double s_soft = swe::dsqrt_rn(x), s_hw = __dsqrt_rn(x);
+    const bool nan_both2 = (s_soft != s_soft) && (s_hw != s_hw);
+    if (!nan_both2 && __double_as_longlong(s_soft) != __double_as_longlong(s_hw)) ++bad_sqrt;
+  }
+  if (bad_div) atomicAdd(counts, bad_div);
+  if (bad_sqrt) atomicAdd(counts + 1, bad_sqrt);
+}
+
+}  // namespace
+
+extern "C" swe_status swe_selftest_fp64(int64_t n, uint64_t seed, int64_t* div_mismatches, int64_t* sqrt_mismatches) {
+  if (n <= 0 || !div_mismatches || !sqrt_mismatches) return SWE_ERR_INVALID_ARGUMENT;
+  unsigned long long* d = nullptr;
+  if (cudaMalloc(&d, 2 * sizeof(unsigned long long)) != cudaSuccess) return SWE_ERR_OUT_OF_MEMORY;
+  cudaMemset(d, 0, 2 * sizeof(unsigned long long));
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  k_fp64_selftest<<<sms * 8, 256>>>(n, seed, d);
+  unsigned long long h[2] = {0, 0};
+  cudaError_t e = cudaMemcpy(h, d, sizeof(h), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (e != cudaSuccess) return SWE_ERR_CUDA;
+  *div_mismatches = (int64_t)h[0];
+  *sqrt_mismatches = (int64_t)h[1];
+  return SWE_OK;
+}

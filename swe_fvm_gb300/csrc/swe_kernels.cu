@@ -71,7 +71,7 @@ __device__ __forceinline__ void write_slot(const DevWork& wk, int slot, double b
 // at a point whose offset term is `off` and whose bathymetry is z.
 __device__ __forceinline__ bool at_point_wet(double w0, double off, double z, double* wout) {
   double a = w0 + off;
-  if ((a - z) >= 0) {
+  if (dge0(a - z)) {
     *wout = a;
     return true;
   }
@@ -88,8 +88,8 @@ __device__ __forceinline__ void node_max(const DevWork& wk, int node, double val
 // PartWet1 level (src/MUSCLObject.cpp:86-112)
 __device__ __forceinline__ double partwet1_level(const double* __restrict__ p, double w, double h) {
   const double b13 = p[0], b23 = p[1], b12 = p[2], bdel = p[3];
-  if (w >= b13) return w;
-  if (w <= bdel) return b23 + cbrt_rn(3. * h * p[6] * p[7]);
+  if (dle(b13, w)) return w;
+  if (dle(w, bdel)) return b23 + cbrt_rn(3. * h * p[6] * p[7]);
   double cc = p[6] * (3. * h * p[8] - p[9]) - p[10];
   (void)b12;
   return bisection(cc, p[5], p[4], p[2], b13);
@@ -129,7 +129,7 @@ __global__ void __launch_bounds__(256) k_recon1(DevMesh m, DevWork wk, const dou
         const int slot = k * C + i;
         write_slot(wk, slot, m.ze[slot], dr[3 + k], 0., 0., dr[6], dr[7], cor);
       }
-    } else if (!(m.fwthr[i] < w)) {
+    } else if (!dlt(m.fwthr[i], w)) {
       // partially wet: PartWet1 now (node maxima), PartWet2 in k_recon2
       const double* p = m.pw1 + (size_t)i * kPw1Stride;
       const double wr = partwet1_level(p, w, h);
@@ -152,7 +152,7 @@ __global__ void __launch_bounds__(256) k_recon1(DevMesh m, DevWork wk, const dou
         const int nb = m.cnbr[k * C + i];  // never a wall: fully-wet cells are interior
         const double wj = W[nb];
         wn[k] = wj;
-        if (m.fwthr[nb] < wj) {
+        if (dlt(m.fwthr[nb], wj)) {
           // fully-wet neighbour: plane point at its centroid
         } else if (!is_wet(wj - m.bc[nb])) {
           first_order = true;
@@ -178,7 +178,7 @@ __global__ void __launch_bounds__(256) k_recon1(DevMesh m, DevWork wk, const dou
           for (int k = 0; k < 3; ++k) {
             const double vmin = smin(w, wn[k]), vmax = smax(w, wn[k]);
             const double vek = w + rec[5 + k];
-            if (!((vmin <= vek) && (vek <= vmax))) tvd = false;
+            if (!(dle(vmin, vek) && dle(vek, vmax))) tvd = false;
           }
           if (tvd) {
             gx = g0;
@@ -236,28 +236,28 @@ __global__ void __launch_bounds__(256) k_recon2(DevMesh m, DevWork wk, const dou
     double w0 = wk.pwrec[i];  // PartWet1 fallback level
     double gx = 0., gy = 0.;
     bool plane = false;
-    if (!((w > b13) || r.flat)) {
+    if (!(dlt(b13, w) || r.flat)) {
       const double w23 = order_val(wk.maxwp[r.lo]);
       const double h23 = w23 - b23;
       const double ratio_b = r.ratio_b;
       const double h_delim1 = 1. / 3. * h23 * ratio_b;
-      const double h_delim2 = 1. / 3. * h23 * r.hd2f / r.d13;
+      const double h_delim2 = SWE_DIV(1. / 3. * h23 * r.hd2f, r.d13);
       const double hi = w - m.bc[i];
-      const double ratio_h = hi / h23;
+      const double ratio_h = SWE_DIV(hi, h23);
       // columns of the reference's `points` after all its writes: point 0 is
       // the lowest vertex with its bathymetry (see the restatement's notes)
       double p1x, p1y, p1z, p2x, p2y, p2z;
       bool ok = true;
-      if (hi <= h_delim1) {
-        const double k2 = sqrt(3. * ratio_h / ratio_b);
+      if (dle(hi, h_delim1)) {
+        const double k2 = SWE_SQRT(SWE_DIV(3. * ratio_h, ratio_b));
         p1x = k2 * r.p[1][0] + (1. - k2) * r.p[0][0];
         p1y = k2 * r.p[1][1] + (1. - k2) * r.p[0][1];
         p1z = k2 * r.p[1][2] + (1. - k2) * r.p[0][2];
-        const double k3 = sqrt(3. * ratio_h * ratio_b);
+        const double k3 = SWE_SQRT(3. * ratio_h * ratio_b);
         p2x = k3 * r.p[2][0] + (1. - k3) * r.p[0][0];
         p2y = k3 * r.p[2][1] + (1. - k3) * r.p[0][1];
         p2z = k3 * r.p[2][2] + (1. - k3) * r.p[0][2];
-      } else if (hi >= h_delim2) {
+      } else if (dle(h_delim2, hi)) {
         const double delta_w = 1.5 * (hi - h_delim2);
         p1x = r.p[1][0]; p1y = r.p[1][1]; p1z = r.p[1][2];
         p2x = r.p[2][0]; p2y = r.p[2][1]; p2z = r.p[2][2];
@@ -265,8 +265,8 @@ __global__ void __launch_bounds__(256) k_recon2(DevMesh m, DevWork wk, const dou
       } else {
         const double alpha = 3. * ratio_h;
         const double beta = r.beta;
-        const double k1 = 1. - bisection((1. + beta - alpha) / (beta * beta), (alpha - 3.) / beta, 0., 0., 1.);
-        if (k1 < kTol) {
+        const double k1 = 1. - bisection(SWE_DIV(1. + beta - alpha, beta * beta), SWE_DIV(alpha - 3., beta), 0., 0., 1.);
+        if (dltc(k1, kTol)) {
           ok = false;
         } else {
           const double bp1 = k1 * b13 + (1. - k1) * b12;
@@ -297,7 +297,7 @@ __global__ void __launch_bounds__(256) k_recon2(DevMesh m, DevWork wk, const dou
 // SpaceDisc::ComputeFluxes with flux plugin FLUX and the CFL min-reduction.
 template <class FLUX, bool BATCH>
 __global__ void __launch_bounds__(256) k_flux(DevMesh m, DevWork wk, const double* __restrict__ W) {
-  __shared__ double s_min[32];
+  __shared__ unsigned long long s_min[32];
   __shared__ int s_inst[32];
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   double lw = kInf;
@@ -326,37 +326,46 @@ __global__ void __launch_bounds__(256) k_flux(DevMesh m, DevWork wk, const doubl
     wk.f1[e] = F[1];
     wk.f2[e] = F[2];
   }
-  // min-reduction of the length-to-wavespeed ratio: warp, block, one atomic
+  // min-reduction of the length-to-wavespeed ratio on order-preserving integer
+  // keys (exact): warp, block, one atomicMin per block and instance
+  const unsigned long long kNone = ~0ull;
+  unsigned long long key = (__double_as_longlong(lw) == __double_as_longlong(kInf)) ? kNone : order_key(lw);
   const int lane = lane_id(), warp = threadIdx.x >> 5;
   const int inst0 = __shfl_sync(0xffffffffu, inst, 0);
   const bool warp_uniform = __all_sync(0xffffffffu, inst == inst0);
   if (warp_uniform) {
 #pragma unroll
-    for (int off = 16; off; off >>= 1) lw = smin(lw, __shfl_xor_sync(0xffffffffu, lw, off));
+    for (int off = 16; off; off >>= 1) {
+      const unsigned long long o = __shfl_xor_sync(0xffffffffu, key, off);
+      key = o < key ? o : key;
+    }
     if (lane == 0) {
-      s_min[warp] = lw;
+      s_min[warp] = key;
       s_inst[warp] = inst0;
     }
   } else {
-    if (lw < kInf) atomicMin(wk.r + inst, order_key(lw));
+    if (key != kNone) atomicMin(wk.r + inst, key);
     if (lane == 0) {
-      s_min[warp] = kInf;
+      s_min[warp] = kNone;
       s_inst[warp] = -1;
     }
   }
   __syncthreads();
   if (warp == 0) {
     const int nw = blockDim.x >> 5;
-    double v = lane < nw ? s_min[lane] : kInf;
+    unsigned long long v = lane < nw ? s_min[lane] : kNone;
     int vi = lane < nw ? s_inst[lane] : s_inst[0];
     const int vi0 = __shfl_sync(0xffffffffu, vi, 0);
-    const bool uni = __all_sync(0xffffffffu, vi == vi0 || v == kInf);
+    const bool uni = __all_sync(0xffffffffu, vi == vi0 || v == kNone);
     if (uni) {
 #pragma unroll
-      for (int off = 16; off; off >>= 1) v = smin(v, __shfl_xor_sync(0xffffffffu, v, off));
-      if (lane == 0 && v < kInf) atomicMin(wk.r + vi0, order_key(v));
-    } else if (v < kInf && vi >= 0) {
-      atomicMin(wk.r + vi, order_key(v));
+      for (int off = 16; off; off >>= 1) {
+        const unsigned long long o = __shfl_xor_sync(0xffffffffu, v, off);
+        v = o < v ? o : v;
+      }
+      if (lane == 0 && v != kNone) atomicMin(wk.r + vi0, v);
+    } else if (v != kNone && vi >= 0) {
+      atomicMin(wk.r + vi, v);
     }
   }
 }
@@ -381,7 +390,7 @@ __global__ void __launch_bounds__(256) k_drain(DevMesh m, DevWork wk, const doub
       const double f = wk.f0[m.cedge[k * m.C + i]];
       sum += smax(0., ((own >> k) & 1u) ? f : -f);
     }
-    d = sum > kTol ? m.area[i] * h / sum : kInf;
+    d = dgtc(sum, kTol) ? SWE_DIV(m.area[i] * h, sum) : kInf;
   }
   wk.drain[i] = d;
 }
@@ -409,7 +418,7 @@ __global__ void __launch_bounds__(256) k_update(DevMesh m, DevWork wk, const dou
     const double F0 = wk.f0[e], F1 = wk.f1[e], F2 = wk.f2[e];
     const int nb = m.cnbr[slot];
     const double dtik = nb < 0 ? kInf : wk.drain[nb];
-    const double dtk = (sgn * F0) > 0. ? smin(dt, dti) : smin(dt, dtik);
+    const double dtk = dgt0(sgn * F0) ? smin(dt, dti) : smin(dt, dtik);
     const double c_ek = m.cek[slot];
     const double h_ek = wk.ew[slot] - m.ze[slot];
     const double s = dtk * sgn * c_ek;

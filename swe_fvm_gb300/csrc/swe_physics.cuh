@@ -10,6 +10,8 @@
 #include <cmath>
 #include <cstdint>
 
+#include "swe_fp64.cuh"
+
 #if defined(__CUDACC__)
 #define SWE_HD __host__ __device__ __forceinline__
 #else
@@ -17,6 +19,16 @@
 #endif
 
 namespace swe {
+
+// Division and square root: the exact integer-pipe routines on the device
+// (bit-identical to IEEE a / b and sqrt), the IEEE operators on the host.
+#if defined(__CUDA_ARCH__)
+#define SWE_DIV(a, b) ::swe::ddiv_rn((a), (b))
+#define SWE_SQRT(x) ::swe::dsqrt_rn((x))
+#else
+#define SWE_DIV(a, b) ((a) / (b))
+#define SWE_SQRT(x) std::sqrt((x))
+#endif
 
 // include/Includes.h:30
 constexpr double kTol = 1e-13;
@@ -30,10 +42,41 @@ constexpr double kEta2 = 1e-6;
 constexpr double kEta4 = 1e-12;
 constexpr double kSqrt2 = 1.4142135623730951;  // std::sqrt(2), correctly rounded
 
-SWE_HD bool is_wet(double h) { return h > kWetDepth; }
-// std::min / std::max (first argument kept on ties and NaN in the second)
-SWE_HD double smin(double a, double b) { return (b < a) ? b : a; }
-SWE_HD double smax(double a, double b) { return (a < b) ? b : a; }
+// ------------------------------------------------------------ comparisons
+// On GB300 a warp-wide FP64 instruction, compares included, occupies the
+// FP64 pipe for ~64 cycles, while the integer pipe issues one per cycle.  On the
+// device every comparison therefore goes through integer keys: for non-NaN
+// doubles, key(x) = (bits < 0) ? -(bits & 0x7FF..F) : bits is monotone and maps
+// -0 and +0 to the same key, so a < b <=> key(a) < key(b) exactly.  (A NaN
+// anywhere makes the state non-finite, which the update kernel reports.)  The
+// host keeps the IEEE comparisons: the two agree on every non-NaN input.
+#if defined(__CUDA_ARCH__)
+__device__ __forceinline__ long long fkey(double x) {
+  const long long i = __double_as_longlong(x);
+  return i < 0 ? -(i & 0x7FFFFFFFFFFFFFFFll) : i;
+}
+__device__ __forceinline__ long long fbits(double x) { return __double_as_longlong(x); }
+SWE_HD bool dlt(double a, double b) { return fkey(a) < fkey(b); }
+SWE_HD bool dle(double a, double b) { return fkey(a) <= fkey(b); }
+// x > c and x < c for a constant c > 0: the signed bit patterns order them
+SWE_HD bool dgtc(double x, double c) { return fbits(x) > fbits(c); }
+SWE_HD bool dltc(double x, double c) { return fbits(x) < fbits(c); }
+// x > 0 and x >= 0
+SWE_HD bool dgt0(double x) { return fbits(x) > 0; }
+SWE_HD bool dge0(double x) { return fkey(x) >= 0; }
+#else
+SWE_HD bool dlt(double a, double b) { return a < b; }
+SWE_HD bool dle(double a, double b) { return a <= b; }
+SWE_HD bool dgtc(double x, double c) { return x > c; }
+SWE_HD bool dltc(double x, double c) { return x < c; }
+SWE_HD bool dgt0(double x) { return x > 0.; }
+SWE_HD bool dge0(double x) { return x >= 0.; }
+#endif
+
+SWE_HD bool is_wet(double h) { return dgtc(h, kWetDepth); }
+// std::min / std::max (first argument kept on ties)
+SWE_HD double smin(double a, double b) { return dlt(b, a) ? b : a; }
+SWE_HD double smax(double a, double b) { return dlt(a, b) ? b : a; }
 
 // ---------------------------------------------------------------- geometry
 // src/PointOperations.cpp:42-48: slope (gx, gy) of the plane through three
@@ -42,18 +85,18 @@ SWE_HD void plane_gradient(double p0x, double p0y, double p0z, double p1x, doubl
                            double p2y, double p2z, double* gx, double* gy) {
   double a00 = p1x - p0x, a01 = p1y - p0y, b0 = p1z - p0z;
   double a10 = p2x - p0x, a11 = p2y - p0y, b1 = p2z - p0z;
-  if (fabs(a10) > fabs(a00)) {
+  if (dlt(fabs(a00), fabs(a10))) {
     double t;
     t = a00; a00 = a10; a10 = t;
     t = a01; a01 = a11; a11 = t;
     t = b0; b0 = b1; b1 = t;
   }
   double l10 = a10;
-  if (a00 != 0.) l10 = a10 / a00;
+  if (a00 != 0.) l10 = SWE_DIV(a10, a00);
   double u11 = a11 - l10 * a01;
   double y1 = b1 - l10 * b0;
-  double x1 = y1 / u11;
-  double x0 = (b0 - a01 * x1) / a00;
+  double x1 = SWE_DIV(y1, u11);
+  double x0 = SWE_DIV(b0 - a01 * x1, a00);
   *gx = x0;
   *gy = x1;
 }
@@ -142,7 +185,7 @@ SWE_HD double cubic(double d, double c, double b, double x) { return x * x * x +
 SWE_HD double bisection(double d, double c, double b, double xmin, double xmax) {
   double fmin_ = cubic(d, c, b, xmin);
   double fmax_ = cubic(d, c, b, xmax);
-  if (signbit(fmin_) == signbit(fmax_)) return (fabs(fmin_) < fabs(fmax_)) ? xmin : xmax;
+  if (signbit(fmin_) == signbit(fmax_)) return dlt(fabs(fmin_), fabs(fmax_)) ? xmin : xmax;
   int n = 50 + trunc_log2(xmax - xmin);
   double x = 0.;
   bool smin_ = signbit(fmin_);
@@ -168,8 +211,8 @@ SWE_HD void prim_assign(double b, double w, double u, double v, double* ow, doub
     *ow = b; *ou = 0.; *ov = 0.;
     return;
   }
-  if (h < kEta1) {
-    double s = kSqrt2 * h / sqrt(h * h + kEta2);
+  if (dltc(h, kEta1)) {
+    double s = SWE_DIV(kSqrt2 * h, SWE_SQRT(h * h + kEta2));
     u *= s;
     v *= s;
   }
@@ -183,8 +226,8 @@ SWE_HD void cons_assign(double b, double h, double hu, double hv, double* ow, do
     return;
   }
   double ih;
-  if (h < kEta1) ih = kSqrt2 * h / sqrt(h * h * h * h + kEta4);
-  else ih = 1. / h;
+  if (dltc(h, kEta1)) ih = SWE_DIV(kSqrt2 * h, SWE_SQRT(h * h * h * h + kEta4));
+  else ih = SWE_DIV(1., h);
   *ow = h + b;
   *ou = hu * ih;
   *ov = hv * ih;
@@ -197,8 +240,9 @@ SWE_HD void elem_flux(double nx, double ny, double h, double hu, double hv, doub
   if (is_wet(h)) {
     double hveln = hu * nx + hv * ny;
     f[0] = hveln;
-    f[1] = (hveln / h) * hu + (0.5 * h * h) * nx;
-    f[2] = (hveln / h) * hv + (0.5 * h * h) * ny;
+    const double q = SWE_DIV(hveln, h);
+    f[1] = q * hu + (0.5 * h * h) * nx;
+    f[2] = q * hv + (0.5 * h * h) * ny;
   }
 }
 
@@ -207,7 +251,7 @@ SWE_HD void elem_flux(double nx, double ny, double h, double hu, double hv, doub
 struct Rusanov {
   static constexpr int id = 0;
   SWE_HD static void speeds(double ul, double hl, double ur, double hr, double* a0, double* a1) {
-    double cl = sqrt(hl), cr = sqrt(hr);
+    double cl = SWE_SQRT(hl), cr = SWE_SQRT(hr);
     double ap = smax(fabs(ul) + cl, fabs(ur) + cr);
     *a0 = -ap;
     *a1 = ap;
@@ -216,7 +260,7 @@ struct Rusanov {
 struct Davis {
   static constexpr int id = 1;
   SWE_HD static void speeds(double ul, double hl, double ur, double hr, double* a0, double* a1) {
-    double cl = sqrt(hl), cr = sqrt(hr);
+    double cl = SWE_SQRT(hl), cr = SWE_SQRT(hr);
     *a0 = smin(ul - cl, ur - cr);
     *a1 = smax(ul + cl, ur + cr);
   }
@@ -224,9 +268,9 @@ struct Davis {
 struct Einfeldt {
   static constexpr int id = 2;
   SWE_HD static void speeds(double ul, double hl, double ur, double hr, double* a0, double* a1) {
-    double cl = sqrt(hl), cr = sqrt(hr);
-    double uRoe = (cl * ul + cl * ur) / (cl + cr);  // the reference's cl * ur
-    double cRoe = sqrt(0.5 * (hl + hr));
+    double cl = SWE_SQRT(hl), cr = SWE_SQRT(hr);
+    double uRoe = SWE_DIV(cl * ul + cl * ur, cl + cr);  // the reference's cl * ur
+    double cRoe = SWE_SQRT(0.5 * (hl + hr));
     *a0 = smin(ul - cl, uRoe - cRoe);
     *a1 = smax(ur + cr, uRoe + cRoe);
   }
@@ -257,20 +301,20 @@ struct HLL {
     double ur = R.u * g.nx + R.v * g.ny;
     double hr = R.w - g.b;
     F[0] = 0.; F[1] = 0.; F[2] = 0.;
-    if (hl + hr <= kMinCapture) return;
+    if (!dgtc(hl + hr, kMinCapture)) return;
     double a0, a1;
     W::speeds(ul, hl, ur, hr, &a0, &a1);
     double al = smin(0., a0);
     double ar = smax(0., a1);
-    if (ar - al <= kMinCapture) return;
-    *lw = g.lmin / (fabs(cor) + smax(-al, ar));
+    if (!dgtc(ar - al, kMinCapture)) return;
+    *lw = SWE_DIV(g.lmin, fabs(cor) + smax(-al, ar));
     double Ul[3] = {hl, hl * L.u, hl * L.v};
     double Ur[3] = {hr, hr * R.u, hr * R.v};
     double Fl[3], Fr[3];
     elem_flux(g.nx, g.ny, Ul[0], Ul[1], Ul[2], Fl);
     elem_flux(g.nx, g.ny, Ur[0], Ur[1], Ur[2], Fr);
 #pragma unroll
-    for (int q = 0; q < 3; ++q) F[q] = (ar * Fl[q] - al * Fr[q] + (al * ar) * (Ur[q] - Ul[q])) / (ar - al);
+    for (int q = 0; q < 3; ++q) F[q] = SWE_DIV(ar * Fl[q] - al * Fr[q] + (al * ar) * (Ur[q] - Ul[q]), ar - al);
   }
 };
 
@@ -287,17 +331,17 @@ struct HLLC {
     double vr = R.u * g.tx + R.v * g.ty;
     double hr = R.w - g.b;
     F[0] = 0.; F[1] = 0.; F[2] = 0.;
-    if (hl + hr <= kMinCapture) return;
+    if (!dgtc(hl + hr, kMinCapture)) return;
     double al, ar;
     W::speeds(ul, hl, ur, hr, &al, &ar);
     double ustar = (ar - ur) * hr * ur - (al - ul) * hl * ul + 0.5 * (hl * hl - hr * hr);
-    ustar /= (hr * (ar - ur) - hl * (al - ul));
-    *lw = g.lmin / (fabs(cor) + smax(kTol, smax(al, ar)));
-    if (ustar <= 0) {
+    ustar = SWE_DIV(ustar, hr * (ar - ur) - hl * (al - ul));
+    *lw = SWE_DIV(g.lmin, fabs(cor) + smax(kTol, smax(al, ar)));
+    if (!dgt0(ustar)) {
       double Ur[3] = {hr, hr * R.u, hr * R.v};
       double us = vr * g.tx + ustar * g.ty;
       double vs = vr * g.nx + ustar * g.ny;
-      double hs = hr * (ar - ur) / (ar - ustar);
+      double hs = SWE_DIV(hr * (ar - ur), ar - ustar);
       double Us[3] = {hs, hs * us, hs * vs};
       double Fr[3];
       elem_flux(g.nx, g.ny, Ur[0], Ur[1], Ur[2], Fr);
@@ -308,7 +352,7 @@ struct HLLC {
       double Ul[3] = {hl, hl * L.u, hl * L.v};
       double us = vl * g.tx + ustar * g.ty;
       double vs = vl * g.nx + ustar * g.ny;
-      double hs = hl * (al - ul) / (al - ustar);
+      double hs = SWE_DIV(hl * (al - ul), al - ustar);
       double Us[3] = {hs, hs * us, hs * vs};
       double Fl[3];
       elem_flux(g.nx, g.ny, Ul[0], Ul[1], Ul[2], Fl);
