@@ -59,12 +59,14 @@ __global__ void k_pack(const double* __restrict__ W, const double* __restrict__ 
   }
 }
 __global__ void k_unpack(const double* __restrict__ in, double* __restrict__ W, double* __restrict__ U,
-                         double* __restrict__ V, int n) {
+                         double* __restrict__ V, int n, unsigned* bad) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) {
-    W[i] = in[3 * i];
-    U[i] = in[3 * i + 1];
-    V[i] = in[3 * i + 2];
+    const double w = in[3 * i], u = in[3 * i + 1], v = in[3 * i + 2];
+    W[i] = w;
+    U[i] = u;
+    V[i] = v;
+    if (bad && !(isfinite(w) && isfinite(u) && isfinite(v))) atomicOr(bad, 1u);
   }
 }
 
@@ -113,18 +115,22 @@ swe_status check_params(const swe_params* p, std::string* why) {
 }
 
 swe_status upload_prim(Engine& eng, const double* prim, int64_t c0, int64_t n, std::string* err) {
-  for (int64_t q = 0; q < 3 * n; ++q)
-    if (!std::isfinite(prim[q]))
-      return fail(err, SWE_ERR_NONFINITE, "state has a non-finite value at cell " + std::to_string(q / 3));
-  // one copy of the interleaved field into the staging buffer, then a device unpack
-  cudaError_t e = cudaMemcpyAsync(eng.d_io, prim, 3 * n * sizeof(double), cudaMemcpyHostToDevice, eng.stream());
+  // one copy of the interleaved field into the staging buffer, then a device
+  // unpack that also flags non-finite values
+  unsigned* flag = eng.d_ioflag;
+  cudaError_t e = cudaMemsetAsync(flag, 0, sizeof(unsigned), eng.stream());
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(eng.d_io, prim, 3 * n * sizeof(double), cudaMemcpyHostToDevice, eng.stream());
   if (e == cudaSuccess) {
     k_unpack<<<(int)((n + 255) / 256), 256, 0, eng.stream()>>>(eng.d_io, eng.state(0, 0) + c0, eng.state(0, 1) + c0,
-                                                                eng.state(0, 2) + c0, (int)n);
+                                                                eng.state(0, 2) + c0, (int)n, flag);
     e = cudaGetLastError();
   }
+  unsigned h = 0;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&h, flag, sizeof(unsigned), cudaMemcpyDeviceToHost, eng.stream());
   if (e == cudaSuccess) e = cudaStreamSynchronize(eng.stream());
   if (e != cudaSuccess) return cuda_fail(err, e, "uploading the state");
+  if (h) return fail(err, SWE_ERR_NONFINITE, "state has a non-finite value");
   return SWE_OK;
 }
 
@@ -336,7 +342,7 @@ swe_status swe_set_prim_device(swe_ctx* ctx, const double* in) {
   if (!ctx || !in) return SWE_ERR_INVALID_ARGUMENT;
   Engine& g = ctx->eng;
   const int n = g.C();
-  k_unpack<<<(n + 255) / 256, 256, 0, g.stream()>>>(in, g.state(0, 0), g.state(0, 1), g.state(0, 2), n);
+  k_unpack<<<(n + 255) / 256, 256, 0, g.stream()>>>(in, g.state(0, 0), g.state(0, 1), g.state(0, 2), n, nullptr);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(&ctx->err, e, "swe_set_prim_device");
   return SWE_OK;

@@ -164,6 +164,7 @@ class Engine {
   // Host copies of the per-instance topology needed by the layout getters.
   std::vector<HostInstance> host;
   double* d_io = nullptr;        // [3C] staging buffer for the interleaved 3 x C field
+  unsigned* d_ioflag = nullptr;  // non-finite flag of the last upload
   double* d_fixed_dt = nullptr;  // device scalar
   double* h_fixed_dt = nullptr;  // pinned host scalar
 

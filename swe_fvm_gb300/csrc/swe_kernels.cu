@@ -572,9 +572,10 @@ std::string Engine::init(std::vector<HostInstance>&& inst, int flux, int ws, int
   Wk.err = dalloc<unsigned>(1);
   for (int q = 0; q < 6; ++q) state_[q] = dalloc<double>(C);
   d_io = dalloc<double>(3 * C);
+  d_ioflag = dalloc<unsigned>(1);
   if (!Wk.ew || !Wk.eu || !Wk.ev || !Wk.sx || !Wk.sy || !Wk.f0 || !Wk.f1 || !Wk.f2 || !Wk.drain || !Wk.maxwp ||
       !Wk.pwlist || !Wk.pwcount || !Wk.pwrec || !Wk.r || !Wk.dt || !Wk.tsum || !d_fixed_dt || !Wk.err ||
-      !state_[5] || !d_io) {
+      !state_[5] || !d_io || !d_ioflag) {
     *st = 6;
     return "device allocation failed";
   }
