@@ -194,6 +194,31 @@ swe_status swe_edge_fluxes_noalloc(int32_t flux, int32_t wavespeed, int64_t n_ed
                                    const double* left, const double* right, double cor, double* flux_out,
                                    double* ratio_out, void* stream);
 
+/* ---------------------------------------------------------- discrete adjoint
+ * No counterpart in the reference.  A taped forward run followed by its exact
+ * reverse gives gradients of any function of gauge traces with respect to the
+ * initial primitive state and the node bathymetry.
+ *
+ * swe_adjoint_forward: n_steps steps of `scheme` from the current state with
+ * dt = CFLdt() before every step (recorded; the gradient treats it as fixed),
+ * state checkpoints every `checkpoint_every` steps (bounded memory), and the
+ * surface level w at the n_gauges cells `gauge_cells` after every
+ * `obs_every`-th step written to traces_out (n_steps / obs_every rows of
+ * n_gauges).  Leaves the context at the final state.
+ *
+ * swe_adjoint_backward: given trace_grads (same shape as the traces: the
+ * derivative of the caller's loss with respect to each trace value), returns
+ * grad_prim0 (3 x C, the initial (w, u, v)) and grad_bathymetry (N, the node
+ * z of the geometry).  Segments are recomputed from their checkpoint with the
+ * recorded dts; the reverse of each stage follows the branches the forward
+ * took (limiter, dry clamps, min/max selections); roots of the partially-wet
+ * reconstruction are differentiated by the implicit-function theorem. */
+swe_status swe_adjoint_forward(swe_ctx* ctx, int32_t scheme, int64_t n_steps, int64_t checkpoint_every,
+                               int32_t n_gauges, const int64_t* gauge_cells, int64_t obs_every, double* traces_out);
+swe_status swe_adjoint_backward(swe_ctx* ctx, const double* trace_grads, double* grad_prim0, double* grad_bathymetry);
+/* The n_steps dts recorded by the last swe_adjoint_forward. */
+swe_status swe_adjoint_dts(swe_ctx* ctx, double* dts_out);
+
 /* ---------------------------------------------------------------- batched */
 /* Many independent instances (each its own mesh, state, parameters and CFL
  * step) stepped together: cells and edges of all instances are concatenated

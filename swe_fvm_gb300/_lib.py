@@ -30,7 +30,7 @@ EXPORTS = [
     "swe_cfl_dt", "swe_min_len_to_wavespeed", "swe_compute_interface_values", "swe_compute_fluxes",
     "swe_get_prim", "swe_set_prim", "swe_get_prim_device", "swe_set_prim_device", "swe_get_edge_values",
     "swe_get_fluxes", "swe_get_node_max", "swe_time_kernels", "swe_measure_fp64_peak", "swe_selftest_fp64", "swe_num_cells", "swe_launch_count", "swe_synchronize",
-    "swe_last_error", "swe_edge_fluxes_noalloc", "swe_batch_create", "swe_batch_destroy", "swe_batch_set_stream", "swe_batch_run_cfl", "swe_batch_run",
+    "swe_last_error", "swe_adjoint_forward", "swe_adjoint_backward", "swe_adjoint_dts", "swe_edge_fluxes_noalloc", "swe_batch_create", "swe_batch_destroy", "swe_batch_set_stream", "swe_batch_run_cfl", "swe_batch_run",
     "swe_batch_get_prim", "swe_batch_time", "swe_batch_launch_count", "swe_batch_synchronize",
     "swe_batch_last_error",
 ]
@@ -112,6 +112,9 @@ def load(build_if_needed: bool = True):
         "swe_synchronize": [vp],
         "swe_last_error": [vp],
         "swe_edge_fluxes_noalloc": [i32, i32, i64, vp, vp, vp, d, vp, vp, vp],
+        "swe_adjoint_forward": [vp, i32, i64, i64, i32, vp, i64, vp],
+        "swe_adjoint_backward": [vp, vp, vp, vp],
+        "swe_adjoint_dts": [vp, vp],
         "swe_batch_create": [i32, vp, vp, P(SweParams), i32, P(vp)],
         "swe_batch_destroy": [vp],
         "swe_batch_set_stream": [vp, vp],

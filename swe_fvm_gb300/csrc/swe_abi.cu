@@ -454,6 +454,43 @@ const char* swe_last_error(swe_ctx* ctx) {
   return ctx->err.c_str();
 }
 
+swe_status swe_adjoint_forward(swe_ctx* ctx, int32_t scheme, int64_t n_steps, int64_t checkpoint_every,
+                               int32_t n_gauges, const int64_t* gauge_cells, int64_t obs_every, double* traces_out) {
+  if (!ctx) return SWE_ERR_INVALID_ARGUMENT;
+  SWE_GUARD_BEGIN
+  if (scheme < 0 || scheme > 2 || n_steps <= 0 || checkpoint_every <= 0 || n_gauges < 0 || obs_every <= 0)
+    return fail(&ctx->err, SWE_ERR_INVALID_ARGUMENT, "bad scheme, step counts or gauge count");
+  if (n_gauges > 0 && (!gauge_cells || !traces_out))
+    return fail(&ctx->err, SWE_ERR_INVALID_ARGUMENT, "gauge_cells and traces_out are required");
+  std::vector<int> g(n_gauges);
+  for (int q = 0; q < n_gauges; ++q) {
+    if (gauge_cells[q] < 0 || gauge_cells[q] >= ctx->eng.C())
+      return fail(&ctx->err, SWE_ERR_INVALID_ARGUMENT, "gauge cell out of range");
+    g[q] = (int)gauge_cells[q];
+  }
+  std::string e = ctx->eng.adjoint_forward(scheme, n_steps, checkpoint_every, g.data(), n_gauges, obs_every,
+                                           traces_out);
+  if (!e.empty()) return fail(&ctx->err, SWE_ERR_CUDA, e);
+  return SWE_OK;
+  SWE_GUARD_END(&ctx->err)
+}
+
+swe_status swe_adjoint_backward(swe_ctx* ctx, const double* trace_grads, double* grad_prim0, double* grad_bathymetry) {
+  if (!ctx || !grad_prim0 || !grad_bathymetry) return SWE_ERR_INVALID_ARGUMENT;
+  SWE_GUARD_BEGIN
+  std::string e = ctx->eng.adjoint_backward(trace_grads, grad_prim0, grad_bathymetry);
+  if (!e.empty()) return fail(&ctx->err, SWE_ERR_INVALID_ARGUMENT, e);
+  return SWE_OK;
+  SWE_GUARD_END(&ctx->err)
+}
+
+swe_status swe_adjoint_dts(swe_ctx* ctx, double* dts_out) {
+  if (!ctx || !dts_out) return SWE_ERR_INVALID_ARGUMENT;
+  std::string e = ctx->eng.adjoint_dts(dts_out);
+  if (!e.empty()) return fail(&ctx->err, SWE_ERR_INVALID_ARGUMENT, e);
+  return SWE_OK;
+}
+
 // ------------------------------------------------------------------ batched
 swe_status swe_batch_create(int32_t n_instances, const swe_mesh* meshes, const double* const* prim0,
                             const swe_params* params, int32_t n_params, swe_batch** out) {

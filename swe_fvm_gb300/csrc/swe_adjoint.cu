@@ -1,0 +1,1027 @@
+// swe_adjoint.cu -- discrete adjoint of the Runge-Kutta step.
+//
+// The reverse of one stage (forward: k_recon1/k_recon2 -> k_flux -> k_drain ->
+// k_update, src/SpaceDisc.cpp:33-74, src/TimeDisc.cpp:3-66,
+// src/Solvers.cpp:5-59) is four kernels, each a gather so that only the rare
+// PartWet2 node-maximum scatter and the bathymetry gradient use atomics:
+//   R1 k_adj_update  cell   RHS + Shu-Osher + ConsAssigner reverse; per slot:
+//                           flux adjoint, draining-dt adjoint and its route
+//   R2 k_adj_drain   cell   gathers the draining-dt adjoint (own slots and the
+//                           neighbours' twin slots), reverses the draining dt
+//   R3 k_adj_flux    edge   gathers both slots' flux adjoints; flux plugin
+//                           reverse by a forward-mode Jacobian (Dual<7>)
+//   R4 k_adj_recon   cell   reconstruction reverse: interface values and
+//                           source gradients to the cell state; bathymetry
+//                           adjoints straight to node z
+// The forward intermediates of the stage (interface slots, fluxes, draining
+// time steps, node maxima) are recomputed from the stage input right before
+// its reverse.  dt is the forward's, frozen: the CFL ratio's dependence on the
+// state is not differentiated.
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "swe_adjoint.cuh"
+#include "swe_dual.cuh"
+
+namespace swe {
+
+namespace {
+
+constexpr double kInfA = __builtin_huge_val();
+
+__device__ __forceinline__ double ldg(const double* p) { return *p; }
+
+// draining time step of the stage (k_drain without the pass reset, so the
+// pass-1 node maxima stay available to the reverse)
+__global__ void __launch_bounds__(256) k_drain_keep(DevMesh m, DevWork wk, const double* __restrict__ W) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m.C) return;
+  const double h = W[i] - m.bc[i];
+  double d;
+  if (!is_wet(h)) {
+    d = 0.;
+  } else {
+    const unsigned own = m.cown[i];
+    double sum = 0.;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const double f = wk.f0[m.cedge[k * m.C + i]];
+      sum += smax(0., ((own >> k) & 1u) ? f : -f);
+    }
+    d = dgtc(sum, kTol) ? SWE_DIV(m.area[i] * h, sum) : kInfA;
+  }
+  wk.drain[i] = d;
+}
+
+__global__ void k_fold_scatter(int C, double* lamp, double* lscatter) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < C) {
+    lamp[i] += lscatter[i];
+    lscatter[i] = 0.;
+  }
+}
+
+__global__ void k_gather_gauges(const double* W, const int* g, int n, double* out) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < n) out[q] = W[g[q]];
+}
+
+// out = a + b (3C arrays)
+__global__ void k_add3(int C, const double* a, const double* b, double* out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < C) {
+    out[i] = a[i] + b[i];
+    out[C + i] = a[C + i] + b[C + i];
+    out[2 * C + i] = a[2 * C + i] + b[2 * C + i];
+  }
+}
+
+__global__ void k_seed_gauges(double* lamw, const int* g, int n, const double* grad) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < n) atomicAdd(lamw + g[q], grad[q]);
+}
+
+// ---------------------------------------------------------------- R1: update
+__global__ void __launch_bounds__(256) k_adj_update(DevMesh m, DevWork wk, AdjWork aw, const double* Wp,
+                                                    const double* Up, const double* Vp, const double* W0,
+                                                    const double* U0, const double* V0, Stage st, int batched) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m.C) return;
+  const int C = m.C;
+  const int inst = batched ? m.cinst[i] : 0;
+  const double dt = st.first ? wk.dt[inst] : st.c * wk.dt[inst];
+  const unsigned own = m.cown[i];
+  const double dti = wk.drain[i];
+  const double b = m.bc[i];
+  // ---- forward recompute of the RHS accumulation and the combination
+  double r0 = 0., r1 = 0., r2 = 0.;
+  double dtk_[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const int slot = k * C + i;
+    const int e = m.cedge[slot];
+    const double sgn = ((own >> k) & 1u) ? 1. : -1.;
+    const double F0 = wk.f0[e], F1 = wk.f1[e], F2 = wk.f2[e];
+    const int nb = m.cnbr[slot];
+    const double dtik = nb < 0 ? kInfA : wk.drain[nb];
+    const double dtk = dgt0(sgn * F0) ? smin(dt, dti) : smin(dt, dtik);
+    dtk_[k] = dtk;
+    const double c_ek = m.cek[slot];
+    const double h_ek = wk.ew[slot] - m.ze[slot];
+    const double s = dtk * sgn * c_ek;
+    r0 -= s * F0;
+    r1 -= s * F1;
+    r2 -= s * F2;
+    const double q = dt * (1. / 3.);
+    r1 -= q * wk.sx[slot] * h_ek;
+    r2 -= q * wk.sy[slot] * h_ek;
+    const double p = 0.5 * h_ek * h_ek;
+    r1 += dtk * (m.cnx[slot] * c_ek * p);
+    r2 += dtk * (m.cny[slot] * c_ek * p);
+  }
+  const double h0 = W0[i] - b;
+  const double c00 = h0, c01 = h0 * U0[i], c02 = h0 * V0[i];
+  double n0, n1, n2, hp = 0., c11 = 0., c12 = 0.;
+  if (st.first) {
+    n0 = c00 + r0;
+    n1 = c01 + r1;
+    n2 = c02 + r2;
+  } else {
+    hp = Wp[i] - b;
+    c11 = hp * Up[i];
+    c12 = hp * Vp[i];
+    n0 = st.a * c00 + st.b * hp + r0;
+    n1 = st.a * c01 + st.b * c11 + r1;
+    n2 = st.a * c02 + st.b * c12 + r2;
+  }
+  // ---- reverse of ConsAssigner (src/Assigners.cpp:28-44)
+  const double lw = aw.lam[i], lu = aw.lam[C + i], lv = aw.lam[2 * C + i];
+  double lbc = 0., ln0 = 0., ln1 = 0., ln2 = 0.;
+  if (!is_wet(n0)) {
+    lbc += lw;
+  } else {
+    double ih, dih;
+    if (dltc(n0, kEta1)) {
+      const double h4 = n0 * n0 * n0 * n0 + kEta4;
+      const double sq = SWE_SQRT(h4);
+      ih = SWE_DIV(kSqrt2 * n0, sq);
+      dih = SWE_DIV(kSqrt2 * (kEta4 - n0 * n0 * n0 * n0), h4 * sq);
+    } else {
+      ih = SWE_DIV(1., n0);
+      dih = -ih * ih;
+    }
+    lbc += lw;
+    ln0 = lw + (lu * n1 + lv * n2) * dih;
+    ln1 = lu * ih;
+    ln2 = lv * ih;
+  }
+  // ---- combination
+  const double a0c = st.first ? 1. : st.a;
+  const double lc00 = a0c * ln0, lc01 = a0c * ln1, lc02 = a0c * ln2;
+  {
+    const double lh0 = lc00 + lc01 * U0[i] + lc02 * V0[i];
+    aw.lam0[i] += lh0;
+    aw.lam0[C + i] += lc01 * h0;
+    aw.lam0[2 * C + i] += lc02 * h0;
+    lbc -= lh0;
+  }
+  if (!st.first) {
+    const double lc10 = st.b * ln0, lc11 = st.b * ln1, lc12 = st.b * ln2;
+    const double lhp = lc10 + lc11 * Up[i] + lc12 * Vp[i];
+    aw.lamp[i] += lhp;
+    aw.lamp[C + i] += lc11 * hp;
+    aw.lamp[2 * C + i] += lc12 * hp;
+    lbc -= lhp;
+  }
+  // ---- reverse of the RHS (src/TimeDisc.cpp:21-36), per local edge
+  const double q = dt * (1. / 3.);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const int slot = k * C + i;
+    const int e = m.cedge[slot];
+    const double sgn = ((own >> k) & 1u) ? 1. : -1.;
+    const double F0 = wk.f0[e], F1 = wk.f1[e], F2 = wk.f2[e];
+    const double c_ek = m.cek[slot];
+    const double h_ek = wk.ew[slot] - m.ze[slot];
+    const double p = 0.5 * h_ek * h_ek;
+    const double dtk = dtk_[k];
+    const double s = dtk * sgn * c_ek;
+    const double nxc = m.cnx[slot] * c_ek, nyc = m.cny[slot] * c_ek;
+    double ldtk = ln1 * (nxc * p) + ln2 * (nyc * p);
+    const double lp = dtk * (ln1 * nxc + ln2 * nyc);
+    double lh = lp * h_ek;
+    aw.lsx[slot] = -ln1 * q * h_ek;
+    aw.lsy[slot] = -ln2 * q * h_ek;
+    lh -= ln1 * q * wk.sx[slot] + ln2 * q * wk.sy[slot];
+    const double ls = -(ln0 * F0 + ln1 * F1 + ln2 * F2);
+    aw.lF0[slot] = -ln0 * s;
+    aw.lF1[slot] = -ln1 * s;
+    aw.lF2[slot] = -ln2 * s;
+    ldtk += ls * sgn * c_ek;
+    aw.lew[slot] = lh;
+    aw.leu[slot] = 0.;
+    aw.lev[slot] = 0.;
+    aw.lze[slot] = -lh;
+    // route of the draining time step actually selected by min(dt, .)
+    const int nb = m.cnbr[slot];
+    int route = 0;
+    if (dgt0(sgn * F0)) {
+      if (dlt(dti, dt)) route = 1;
+    } else if (nb >= 0) {
+      if (dlt(wk.drain[nb], dt)) route = 2;
+    }
+    aw.ldtk[slot] = route ? ldtk : 0.;
+    aw.route[slot] = (unsigned char)route;
+  }
+  aw.lbc[i] = lbc;
+}
+
+// ---------------------------------------------------------------- R2: drain
+__global__ void __launch_bounds__(256) k_adj_drain(DevMesh m, DevWork wk, AdjWork aw, const double* Wp) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m.C) return;
+  const int C = m.C;
+  double ld = 0.;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const int slot = k * C + i;
+    if (aw.route[slot] == 1) ld += aw.ldtk[slot];
+    const int tw = aw.twin[slot];
+    if (tw >= 0 && aw.route[tw] == 2) ld += aw.ldtk[tw];
+  }
+  const double h = Wp[i] - m.bc[i];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) aw.lF0d[k * C + i] = 0.;
+  if (ld == 0. || !is_wet(h)) return;
+  const unsigned own = m.cown[i];
+  double sum = 0.;
+  double fk[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const double f = wk.f0[m.cedge[k * C + i]];
+    fk[k] = ((own >> k) & 1u) ? f : -f;
+    sum += smax(0., fk[k]);
+  }
+  if (!dgtc(sum, kTol)) return;
+  const double A = m.area[i];
+  const double d = SWE_DIV(A * h, sum);
+  const double lAh = SWE_DIV(ld, sum);
+  const double ls = -SWE_DIV(ld * d, sum);
+  const double lh = lAh * A;
+  aw.lamp[i] += lh;
+  aw.lbc[i] -= lh;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    if (dlt(0., fk[k])) aw.lF0d[k * C + i] = ((own >> k) & 1u) ? ls : -ls;
+  }
+}
+
+// ---------------------------------------------------------------- R3: flux
+template <int FLUX, int WS>
+__global__ void __launch_bounds__(256) k_adj_flux(DevMesh m, DevWork wk, AdjWork aw, const double* Wp) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= m.E) return;
+  const int o = m.eown[e], nb = m.enb[e];
+  const int sl = m.eslotl[e];
+  double lF[3] = {aw.lF0[sl] + aw.lF0d[sl], aw.lF1[sl], aw.lF2[sl]};
+  const double nx = m.enx[e], ny = m.eny[e];
+  if (nb < 0) {
+    // wall: F = ElemFlux(n, (h_owner, 0, 0)) -> dF/dh = (0, h nx, h ny)
+    const double h = Wp[o] - m.bc[o];
+    aw.lhwall[sl] = is_wet(h) ? (lF[1] * nx + lF[2] * ny) * h : 0.;
+    return;
+  }
+  aw.lhwall[sl] = 0.;
+  const int sr = m.eslotr[e];
+  lF[0] += aw.lF0[sr] + aw.lF0d[sr];
+  lF[1] += aw.lF1[sr];
+  lF[2] += aw.lF2[sr];
+  if (lF[0] == 0. && lF[1] == 0. && lF[2] == 0.) return;
+  typedef Dual<7> D;
+  D Lw = D::var(wk.ew[sl], 0), Lu = D::var(wk.eu[sl], 1), Lv = D::var(wk.ev[sl], 2);
+  D Rw = D::var(wk.ew[sr], 3), Ru = D::var(wk.eu[sr], 4), Rv = D::var(wk.ev[sr], 5);
+  D b = D::var(m.ezm[e], 6);
+  D F[3];
+  flux_t(FLUX, WS, nx, ny, m.etx[e], m.ety[e], b, Lw, Lu, Lv, Rw, Ru, Rv, F);
+  double g[7];
+#pragma unroll
+  for (int k = 0; k < 7; ++k) g[k] = lF[0] * F[0].d[k] + lF[1] * F[1].d[k] + lF[2] * F[2].d[k];
+  aw.lew[sl] += g[0];
+  aw.leu[sl] += g[1];
+  aw.lev[sl] += g[2];
+  aw.lew[sr] += g[3];
+  aw.leu[sr] += g[4];
+  aw.lev[sr] += g[5];
+  aw.lze[sl] += g[6];
+}
+
+// ------------------------------------------------------- R4: reconstruction
+// Pass-1 reconstruction of cell c restated for the reverse: type 0 dry,
+// 1 partially wet (PartWet1 level in w0), 2 fully wet; for fully wet: the
+// combination mask and whether the plane survived positivity and the limiter.
+struct P1 {
+  int type, mask;
+  bool kept;
+  double w0;
+};
+__device__ P1 pass1(const DevMesh& m, const double* W, int c) {
+  P1 r{0, 0, false, 0.};
+  const int C = m.C;
+  const double w = W[c];
+  const double h = w - m.bc[c];
+  if (!is_wet(h)) return r;
+  if (!dlt(m.fwthr[c], w)) {
+    r.type = 1;
+    const double* p = m.pw1 + (size_t)c * kPw1Stride;
+    const double b13 = p[0], b23 = p[1], bdel = p[3];
+    if (dle(b13, w)) r.w0 = w;
+    else if (dle(w, bdel)) r.w0 = b23 + cbrt_rn(3. * h * p[6] * p[7]);
+    else r.w0 = bisection(p[6] * (3. * h * p[8] - p[9]) - p[10], p[5], p[4], p[2], b13);
+    return r;
+  }
+  r.type = 2;
+  r.w0 = w;
+  bool first_order = false;
+  double wn[3];
+  for (int k = 0; k < 3; ++k) {
+    const int nb = m.cnbr[k * C + c];
+    const double wj = W[nb];
+    wn[k] = wj;
+    if (dlt(m.fwthr[nb], wj)) {
+    } else if (!is_wet(wj - m.bc[nb])) {
+      first_order = true;
+    } else {
+      r.mask |= 1 << k;
+    }
+  }
+  if (first_order) return r;
+  const double* rec = m.combo + ((size_t)c * 8 + r.mask) * kComboStride;
+  for (int k = 0; k < 3; ++k)
+    if (!is_wet((rec[2 + k] + w) - m.zn[k * C + c])) return r;
+  for (int k = 0; k < 3; ++k) {
+    const double vek = w + rec[5 + k];
+    if (!(dle(smin(w, wn[k]), vek) && dle(vek, smax(w, wn[k])))) return r;
+  }
+  r.kept = true;
+  return r;
+}
+
+// Pass-1 value of cell c at its local node kn (AtPoint(P).w), and where its
+// derivative goes: dstate = d value / d W[c]; static part to node z.
+__device__ double pass1_node_value(const DevMesh& m, const double* W, int c, int kn) {
+  const int C = m.C;
+  const double z = m.zn[kn * C + c];
+  const P1 p = pass1(m, W, c);
+  if (p.type == 0) return m.dry[(size_t)c * kDryStride + kn];
+  double off = 0.;
+  if (p.type == 2 && p.kept) off = m.combo[((size_t)c * 8 + p.mask) * kComboStride + 8 + kn];
+  const double a = p.w0 + off;
+  return dge0(a - z) ? a : z;
+}
+
+// node id of local node k of cell c
+__device__ __forceinline__ int cnode(const DevMesh& m, int c, int k) { return m.cnode[k * m.C + c]; }
+
+// adds l to the node-z gradient through the edge-centre bathymetry of slot
+// (c, k): the midpoint of the edge's two nodes
+__device__ __forceinline__ void lam_edge_z(const DevMesh& m, AdjWork& aw, int c, int k, double l) {
+  if (l == 0.) return;
+  const int e = m.cedge[k * m.C + c];
+  atomicAdd(aw.lz + aw.edge_nodes[2 * e], 0.5 * l);
+  atomicAdd(aw.lz + aw.edge_nodes[2 * e + 1], 0.5 * l);
+}
+// ... through the centroid bathymetry of cell c
+__device__ __forceinline__ void lam_cell_z(const DevMesh& m, AdjWork& aw, int c, double l) {
+  if (l == 0.) return;
+  const double k3 = 1. / 3.;
+  for (int k = 0; k < 3; ++k) atomicAdd(aw.lz + cnode(m, c, k), k3 * l);
+}
+
+// PartWet1 level and its derivatives with respect to (w, z0, z1, z2) of the
+// cell (src/MUSCLObject.cpp:86-112), recomputed from the node bathymetry.
+template <class T>
+__device__ T partwet1_t(const T& w, const T& z0, const T& z1, const T& z2) {
+  const double k3 = 1. / 3.;
+  T bc = z0 * k3 + z1 * k3 + z2 * k3;
+  T h = w - bc;
+  T b13 = z0, b23 = z0;
+  if (dlt(val(b13), val(z1))) b13 = z1;
+  if (dlt(val(b13), val(z2))) b13 = z2;
+  if (dlt(val(z1), val(b23))) b23 = z1;
+  if (dlt(val(z2), val(b23))) b23 = z2;
+  T b12 = 3. * bc - b23 - b13;
+  T bdel = b12 + (1. / 3.) * (b13 - b12) * (b13 - b12) / (b13 - b23);
+  if (dle(val(b13), val(w))) return w;
+  if (dle(val(w), val(bdel))) return b23 + tcbrt(3. * h * (b13 - b23) * (b12 - b23));
+  T a = -3. * b13;
+  T bb = 3. * (b12 * b13 + b13 * b23 - b12 * b23);
+  T cc = (b13 - b23) * (3. * h * (b13 - b12) - b12 * (b12 + b23)) - b23 * b23 * b13;
+  return bisection_t(cc, bb, a, val(b12), val(b13));
+}
+
+// PartWet2 (src/MUSCLObject.cpp:114-191) recomputed from the sorted vertices
+// with dual (w, w23, z_lo, z_mid, z_hi): level at the centroid and slope.
+// Returns false if it falls back to PartWet1.
+template <class T>
+__device__ bool partwet2_t(const Pw2Rec& r, const T& w, const T& w23, const T& zl, const T& zm, const T& zh,
+                           const T& bc, T* w0, T* gx, T* gy) {
+  T b23 = zl, b12 = zm, b13 = zh;
+  if (dlt(val(b13), val(w)) || r.flat) return false;
+  T h23 = w23 - b23;
+  T ratio_b = (b12 - b23) / (b13 - b23);
+  T h_delim1 = 1. / 3. * h23 * ratio_b;
+  T h_delim2 = 1. / 3. * h23 * (2. * b13 - b12 - b23) / (b13 - b23);
+  T hi = w - bc;
+  T ratio_h = hi / h23;
+  const T P0x(r.p[0][0]), P0y(r.p[0][1]), P1x(r.p[1][0]), P1y(r.p[1][1]), P2x(r.p[2][0]), P2y(r.p[2][1]);
+  T p1x, p1y, p1z, p2x, p2y, p2z;
+  if (dle(val(hi), val(h_delim1))) {
+    T k2 = tsqrt(3. * ratio_h / ratio_b);
+    p1x = k2 * P1x + (1. - k2) * P0x;
+    p1y = k2 * P1y + (1. - k2) * P0y;
+    p1z = k2 * zm + (1. - k2) * zl;
+    T k3 = tsqrt(3. * ratio_h * ratio_b);
+    p2x = k3 * P2x + (1. - k3) * P0x;
+    p2y = k3 * P2y + (1. - k3) * P0y;
+    p2z = k3 * zh + (1. - k3) * zl;
+  } else if (dle(val(h_delim2), val(hi))) {
+    T delta_w = 1.5 * (hi - h_delim2);
+    p1x = P1x; p1y = P1y; p1z = zm;
+    p2x = P2x; p2y = P2y; p2z = zh;
+    p2z = p2z + delta_w;
+  } else {
+    T alpha = 3. * ratio_h;
+    T beta = (b13 - b12) / (b13 - b23);
+    T k1 = 1. - bisection_t((1. + beta - alpha) / (beta * beta), (alpha - 3.) / beta, T(0.), 0., 1.);
+    if (dltc(val(k1), kTol)) return false;
+    T bp1 = k1 * b13 + (1. - k1) * b12;
+    p1x = P1x; p1y = P1y; p1z = zm;
+    p2x = k1 * P2x + (1. - k1) * P1x;
+    p2y = k1 * P2y + (1. - k1) * P1y;
+    p2z = bp1;
+  }
+  plane_gradient_t(P0x, P0y, zl, p1x, p1y, p1z, p2x, p2y, p2z, gx, gy);
+  *w0 = w23 + (*gx * r.tp0x + *gy * r.tp0y);
+  return true;
+}
+
+// reverse of one interface slot write (src/SpaceDisc.cpp:24-29): given the
+// adjoints of the slot (w, u, v, sx, sy) and the forward inputs of AtPoint,
+// returns adjoints of (w0 + off) [law], u0, v0, gx, gy, and of the slot's
+// edge bathymetry (ze).
+__device__ void slot_reverse(double ze, double a_w, double u0, double v0, double cor, double lw, double lu, double lv,
+                             double lsx, double lsy, double* law, double* lu0, double* lv0, double* lgx, double* lgy,
+                             double* lze) {
+  *lgx = lsx;
+  *lgy = lsy;
+  // AtPoint dry check
+  double aw_ = a_w, au = u0, av = v0;
+  const bool wet_at = dge0(a_w - ze);
+  if (!wet_at) {
+    aw_ = ze;
+    au = 0.;
+    av = 0.;
+  }
+  // src += cor (-v, u) uses the assigned velocities
+  double lue = lu + cor * lsy, lve = lv - cor * lsx;
+  double law_ = 0., lau = 0., lav = 0., lz = 0.;
+  const double h = aw_ - ze;
+  if (!is_wet(h)) {
+    lz += lw;
+  } else {
+    law_ = lw;
+    if (dltc(h, kEta1)) {
+      const double t = h * h + kEta2;
+      const double st = SWE_SQRT(t);
+      const double s = SWE_DIV(kSqrt2 * h, st);
+      const double ds = SWE_DIV(kSqrt2 * kEta2, t * st);
+      lau = lue * s;
+      lav = lve * s;
+      const double lh = (lue * au + lve * av) * ds;
+      law_ += lh;
+      lz -= lh;
+    } else {
+      lau = lue;
+      lav = lve;
+    }
+  }
+  if (wet_at) {
+    *law = law_;
+    *lu0 = lau;
+    *lv0 = lav;
+  } else {
+    *law = 0.;
+    *lu0 = 0.;
+    *lv0 = 0.;
+    lz += law_;
+  }
+  *lze = lz;
+}
+
+__global__ void __launch_bounds__(256) k_adj_recon(DevMesh m, DevWork wk, AdjWork aw, const double* W,
+                                                   const double* U, const double* V, int batched) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m.C) return;
+  const int C = m.C;
+  const int inst = batched ? m.cinst[i] : 0;
+  const double cor = m.inst_cor[inst];
+  const double w = W[i], u = U[i], v = V[i];
+  double lw_i = 0., lu_i = 0., lv_i = 0.;
+  double lbc = aw.lbc[i];
+  // wall-flux depth adjoints of the owned wall edges
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const double lh = aw.lhwall[k * C + i];
+    if (lh != 0. && m.cnbr[k * C + i] < 0 && ((m.cown[i] >> k) & 1u)) {
+      lw_i += lh;
+      lbc -= lh;
+    }
+  }
+  const P1 p = pass1(m, W, i);
+  // forward description of the final interface values: level w0 + off_k, velocity, slope
+  double w0 = w, gx = 0., gy = 0., off[3] = {0., 0., 0.};
+  double u0 = u, v0 = v;
+  bool pw2_plane = false;
+  double w23 = 0.;
+  int lo_node = -1;
+  if (p.type == 0) {
+    const double* dr = m.dry + (size_t)i * kDryStride;
+    // interface values (dew_k, 0, 0) and slope (sx, sy): all bathymetry
+    for (int k = 0; k < 3; ++k) {
+      const int slot = k * C + i;
+      double law, lu0, lv0, lgx, lgy, lze;
+      slot_reverse(m.ze[slot], dr[3 + k], 0., 0., cor, aw.lew[slot], aw.leu[slot], aw.lev[slot], aw.lsx[slot],
+                   aw.lsy[slot], &law, &lu0, &lv0, &lgx, &lgy, &lze);
+      lze += aw.lze[slot];
+      // dew_k and (sx, sy) as functions of the cell's node z: dual over z0..z2
+      typedef Dual<3> D;
+      D z0 = D::var(m.zn[i], 0), z1 = D::var(m.zn[C + i], 1), z2 = D::var(m.zn[2 * C + i], 2);
+      const Pw2Rec& r = m.pw2[i];
+      // node positions in cell order from dnode (P_k - T) and T: recover P_k = T + dnode_k
+      // (T is never needed: slopes depend on differences only)
+      D sxd, syd;
+      plane_gradient_t(D(r.dnode[0][0]), D(r.dnode[0][1]), z0, D(r.dnode[1][0]), D(r.dnode[1][1]), z1,
+                       D(r.dnode[2][0]), D(r.dnode[2][1]), z2, &sxd, &syd);
+      const double k3 = 1. / 3.;
+      D bcd = z0 * k3 + z1 * k3 + z2 * k3;
+      D e0v = bcd + (sxd * r.dedge[k][0] + syd * r.dedge[k][1]);
+      double lz3[3];
+      for (int q = 0; q < 3; ++q) lz3[q] = law * e0v.d[q] + lgx * sxd.d[q] + lgy * syd.d[q];
+      for (int q = 0; q < 3; ++q)
+        if (lz3[q] != 0.) atomicAdd(aw.lz + cnode(m, i, q), lz3[q]);
+      lam_edge_z(m, aw, i, k, lze);
+    }
+    lam_cell_z(m, aw, i, lbc);
+    return;
+  }
+  if (p.type == 2) {
+    w0 = w;
+    if (p.kept) {
+      const double* rec = m.combo + ((size_t)i * 8 + p.mask) * kComboStride;
+      gx = rec[0];
+      gy = rec[1];
+      for (int k = 0; k < 3; ++k) off[k] = rec[5 + k];
+    }
+  } else {
+    // partially wet: PartWet2 with the pass-1 maxima, else PartWet1
+    const Pw2Rec& r = m.pw2[i];
+    lo_node = r.lo;
+    w23 = order_val(wk.maxwp[r.lo]);
+    const double bcv = m.bc[i];
+    double w0d, gxd, gyd;
+    pw2_plane = partwet2_t(r, w, w23, r.p[0][2], r.p[1][2], r.p[2][2], bcv, &w0d, &gxd, &gyd);
+    if (pw2_plane) {
+      w0 = w0d;
+      gx = gxd;
+      gy = gyd;
+      for (int k = 0; k < 3; ++k) off[k] = gx * r.dedge[k][0] + gy * r.dedge[k][1];
+    } else {
+      w0 = p.w0;
+    }
+  }
+  // slot reverses
+  double lw0 = 0., lgx = 0., lgy = 0., loff[3];
+  for (int k = 0; k < 3; ++k) {
+    const int slot = k * C + i;
+    double law, lu0, lv0, lgxk, lgyk, lze;
+    slot_reverse(m.ze[slot], w0 + off[k], u0, v0, cor, aw.lew[slot], aw.leu[slot], aw.lev[slot], aw.lsx[slot],
+                 aw.lsy[slot], &law, &lu0, &lv0, &lgxk, &lgyk, &lze);
+    lw0 += law;
+    loff[k] = law;
+    lu_i += lu0;
+    lv_i += lv0;
+    lgx += lgxk;
+    lgy += lgyk;
+    lam_edge_z(m, aw, i, k, lze + aw.lze[slot]);
+  }
+  if (p.type == 2) {
+    lw_i += lw0;
+    if (p.kept) {
+      // the combination plane through neighbour centroids / edge centres
+      typedef Dual<3> D;
+      D pz[3];
+      double px[3], py[3];
+      const Pw2Rec& r = m.pw2[i];
+      for (int k = 0; k < 3; ++k) {
+        const int nb = m.cnbr[k * C + i];
+        if ((p.mask >> k) & 1) {
+          pz[k] = D::var(m.ze[k * C + i], k);
+          px[k] = r.dedge[k][0];
+          py[k] = r.dedge[k][1];
+        } else {
+          pz[k] = D::var(m.bc[nb], k);
+          // neighbour centroid relative to this cell's centroid
+          const Pw2Rec& rn = m.pw2[nb];
+          px[k] = (rn.p[0][0] + rn.tp0x) - (r.p[0][0] + r.tp0x);
+          py[k] = (rn.p[0][1] + rn.tp0y) - (r.p[0][1] + r.tp0y);
+        }
+      }
+      D g0, g1;
+      plane_gradient_t(D(px[0]), D(py[0]), pz[0], D(px[1]), D(py[1]), pz[1], D(px[2]), D(py[2]), pz[2], &g0, &g1);
+      // off_k = g0 dEx + g1 dEy
+      double lg0 = lgx, lg1 = lgy;
+      for (int k = 0; k < 3; ++k) {
+        lg0 += loff[k] * r.dedge[k][0];
+        lg1 += loff[k] * r.dedge[k][1];
+      }
+      for (int k = 0; k < 3; ++k) {
+        const double lp = lg0 * g0.d[k] + lg1 * g1.d[k];
+        if (lp == 0.) continue;
+        if ((p.mask >> k) & 1) lam_edge_z(m, aw, i, k, lp);
+        else lam_cell_z(m, aw, m.cnbr[k * C + i], lp);
+      }
+    }
+  } else {
+    const Pw2Rec& r = m.pw2[i];
+    int sorted_local[3] = {r.sk[0], r.sk[1], r.sk[2]};
+    if (pw2_plane) {
+      typedef Dual<5> D;
+      D wd = D::var(w, 0), w23d = D::var(w23, 1);
+      D zl = D::var(r.p[0][2], 2), zm = D::var(r.p[1][2], 3), zh = D::var(r.p[2][2], 4);
+      const double k3 = 1. / 3.;
+      // bc as a function of the three node z (in cell order)
+      D zc[3];
+      for (int k = 0; k < 3; ++k) zc[k] = D(m.zn[k * C + i]);
+      for (int s = 0; s < 3; ++s) zc[sorted_local[s]] = (s == 0) ? zl : (s == 1 ? zm : zh);
+      D bcd = zc[0] * k3 + zc[1] * k3 + zc[2] * k3;
+      D w0d, gxd, gyd;
+      partwet2_t(r, wd, w23d, zl, zm, zh, bcd, &w0d, &gxd, &gyd);
+      double lg0 = lgx, lg1 = lgy;
+      for (int k = 0; k < 3; ++k) {
+        lg0 += loff[k] * r.dedge[k][0];
+        lg1 += loff[k] * r.dedge[k][1];
+      }
+      double g[5];
+      for (int q = 0; q < 5; ++q) g[q] = lw0 * w0d.d[q] + lg0 * gxd.d[q] + lg1 * gyd.d[q];
+      lw_i += g[0];
+      // node z of the sorted vertices
+      for (int s = 0; s < 3; ++s)
+        if (g[2 + s] != 0.) atomicAdd(aw.lz + cnode(m, i, sorted_local[s]), g[2 + s]);
+      // w23 = max over the cells around the lowest node of their pass-1 value
+      if (g[1] != 0.) {
+        const int nd = lo_node;
+        int best = -1, bestk = 0;
+        for (int q = aw.node_ptr[nd]; q < aw.node_ptr[nd + 1]; ++q) {
+          const int c = aw.node_cells[q] >> 2, kn = aw.node_cells[q] & 3;
+          const double val_c = pass1_node_value(m, W, c, kn);
+          if (val_c == w23) {
+            best = c;
+            bestk = kn;
+            break;
+          }
+        }
+        if (best < 0) {
+          atomicAdd(aw.lz + nd, g[1]);  // the maximum is the node bathymetry itself
+        } else {
+          const P1 pc = pass1(m, W, best);
+          const double zc_ = m.zn[bestk * C + best];
+          if (pc.type == 0) {
+            // dry plane value at the node: a function of bathymetry only
+            typedef Dual<3> E;
+            const Pw2Rec& rb = m.pw2[best];
+            E z0 = E::var(m.zn[best], 0), z1 = E::var(m.zn[C + best], 1), z2 = E::var(m.zn[2 * C + best], 2);
+            E sxd, syd;
+            plane_gradient_t(E(rb.dnode[0][0]), E(rb.dnode[0][1]), z0, E(rb.dnode[1][0]), E(rb.dnode[1][1]), z1,
+                             E(rb.dnode[2][0]), E(rb.dnode[2][1]), z2, &sxd, &syd);
+            E bcb = z0 * k3 + z1 * k3 + z2 * k3;
+            E a = bcb + (sxd * rb.dnode[bestk][0] + syd * rb.dnode[bestk][1]);
+            if (dge0(a.v - zc_)) {
+              for (int q = 0; q < 3; ++q) atomicAdd(aw.lz + cnode(m, best, q), g[1] * a.d[q]);
+            } else {
+              atomicAdd(aw.lz + cnode(m, best, bestk), g[1]);
+            }
+          } else {
+            double off_n = 0.;
+            if (pc.type == 2 && pc.kept) off_n = m.combo[((size_t)best * 8 + pc.mask) * kComboStride + 8 + bestk];
+            const double a = pc.w0 + off_n;
+            if (!dge0(a - zc_)) {
+              atomicAdd(aw.lz + cnode(m, best, bestk), g[1]);
+            } else if (pc.type == 2) {
+              atomicAdd(aw.lscatter + best, g[1]);  // w of a fully-wet cell (+ bathymetry offset, not tracked)
+            } else {
+              typedef Dual<4> F4;
+              F4 wb = F4::var(W[best], 0);
+              F4 y = partwet1_t(wb, F4::var(m.zn[best], 1), F4::var(m.zn[C + best], 2), F4::var(m.zn[2 * C + best], 3));
+              atomicAdd(aw.lscatter + best, g[1] * y.d[0]);
+              for (int q = 0; q < 3; ++q)
+                if (y.d[1 + q] != 0.) atomicAdd(aw.lz + cnode(m, best, q), g[1] * y.d[1 + q]);
+            }
+          }
+        }
+      }
+    } else {
+      // PartWet1 level: dual over (w, z0, z1, z2)
+      typedef Dual<4> D;
+      D y = partwet1_t(D::var(w, 0), D::var(m.zn[i], 1), D::var(m.zn[C + i], 2), D::var(m.zn[2 * C + i], 3));
+      lw_i += lw0 * y.d[0];
+      for (int q = 0; q < 3; ++q)
+        if (y.d[1 + q] != 0.) atomicAdd(aw.lz + cnode(m, i, q), lw0 * y.d[1 + q]);
+    }
+  }
+  aw.lamp[i] += lw_i;
+  aw.lamp[C + i] += lu_i;
+  aw.lamp[2 * C + i] += lv_i;
+  lam_cell_z(m, aw, i, lbc);
+}
+
+}  // namespace
+
+// ----------------------------------------------------------------- driver
+struct AdjointState {
+  AdjWork aw{};
+  std::vector<void*> allocs;
+  // tape of the last taped forward run
+  int scheme = 1;
+  int64_t n_steps = 0, ckpt = 0, obs = 0;
+  int n_gauges = 0;
+  int* d_gauges = nullptr;
+  std::vector<double*> checkpoints;  // [3C] state at steps 0, ckpt, 2 ckpt, ...
+  double* d_dt = nullptr;            // [n_steps] recorded dt
+  double* d_traces = nullptr;        // [n_obs x n_gauges]
+  bool taped = false;
+  template <class T>
+  T* alloc(size_t n) {
+    void* p = nullptr;
+    if (cudaMalloc(&p, (n ? n : 1) * sizeof(T)) != cudaSuccess) return nullptr;
+    allocs.push_back(p);
+    return (T*)p;
+  }
+  void free_tape() {
+    for (double* p : checkpoints) cudaFree(p);
+    checkpoints.clear();
+    if (d_dt) cudaFree(d_dt);
+    if (d_traces) cudaFree(d_traces);
+    if (d_gauges) cudaFree(d_gauges);
+    d_dt = d_traces = nullptr;
+    d_gauges = nullptr;
+    taped = false;
+  }
+  ~AdjointState() {
+    free_tape();
+    for (void* p : allocs) cudaFree(p);
+  }
+};
+
+void adjoint_state_delete(AdjointState* a) { delete a; }
+
+std::string Engine::adjoint_init() {
+  if (adj_) return "";
+  if (I() != 1) return "the adjoint runs on a single-instance context";
+  AdjointState* a = new AdjointState();
+  const int64_t C = mesh_.C, E = mesh_.E, N = mesh_.N;
+  AdjWork& w = a->aw;
+  bool ok = true;
+  auto A = [&](double*& p, size_t n) {
+    p = a->alloc<double>(n);
+    ok = ok && p;
+  };
+  A(w.lam, 3 * C); A(w.lamp, 3 * C); A(w.lam0, 3 * C);
+  A(w.lew, 3 * C); A(w.leu, 3 * C); A(w.lev, 3 * C); A(w.lsx, 3 * C); A(w.lsy, 3 * C); A(w.lze, 3 * C);
+  A(w.lF0, 3 * C); A(w.lF1, 3 * C); A(w.lF2, 3 * C); A(w.lF0d, 3 * C); A(w.ldtk, 3 * C); A(w.lhwall, 3 * C);
+  A(w.lbc, C); A(w.lscatter, C); A(w.lz, N);
+  w.route = a->alloc<unsigned char>(3 * C);
+  ok = ok && w.route;
+  // twin slots, node -> cells, edge nodes (host, from the instance's topology)
+  const HostInstance& h = host[0];
+  std::vector<int> twin(3 * C, -1), eown_k(E, -1), enb_k(E, -1), en(2 * E);
+  for (int64_t e = 0; e < E; ++e) {
+    en[2 * e] = (int)h.en[2 * e];
+    en[2 * e + 1] = (int)h.en[2 * e + 1];
+  }
+  for (int64_t i = 0; i < C; ++i)
+    for (int k = 0; k < 3; ++k) {
+      const int64_t e = h.ce[3 * i + k];
+      if (h.ec[2 * e] == i) eown_k[e] = (int)(k * C + i);
+      else enb_k[e] = (int)(k * C + i);
+    }
+  for (int64_t e = 0; e < E; ++e)
+    if (eown_k[e] >= 0 && enb_k[e] >= 0) {
+      twin[eown_k[e]] = enb_k[e];
+      twin[enb_k[e]] = eown_k[e];
+    }
+  std::vector<int> ptr(N + 1, 0), cells(3 * C);
+  for (int64_t i = 0; i < C; ++i)
+    for (int k = 0; k < 3; ++k) ptr[h.cn[3 * i + k] + 1]++;
+  for (int64_t n = 0; n < N; ++n) ptr[n + 1] += ptr[n];
+  std::vector<int> fill(ptr.begin(), ptr.end() - 1);
+  for (int64_t i = 0; i < C; ++i)
+    for (int k = 0; k < 3; ++k) cells[fill[h.cn[3 * i + k]]++] = (int)((i << 2) | k);
+  int* d_twin = a->alloc<int>(3 * C);
+  int* d_ptr = a->alloc<int>(N + 1);
+  int* d_cells = a->alloc<int>(3 * C);
+  int* d_en = a->alloc<int>(2 * E);
+  ok = ok && d_twin && d_ptr && d_cells && d_en;
+  if (!ok) {
+    delete a;
+    return "adjoint work allocation failed";
+  }
+  cudaMemcpy(d_twin, twin.data(), 3 * C * sizeof(int), cudaMemcpyHostToDevice);
+  cudaMemcpy(d_ptr, ptr.data(), (N + 1) * sizeof(int), cudaMemcpyHostToDevice);
+  cudaMemcpy(d_cells, cells.data(), 3 * C * sizeof(int), cudaMemcpyHostToDevice);
+  cudaMemcpy(d_en, en.data(), 2 * E * sizeof(int), cudaMemcpyHostToDevice);
+  w.twin = d_twin;
+  w.node_ptr = d_ptr;
+  w.node_cells = d_cells;
+  w.edge_nodes = d_en;
+  cudaMemset(w.lscatter, 0, C * sizeof(double));
+  adj_ = a;
+  return "";
+}
+
+std::string Engine::adjoint_forward(int scheme, int64_t n_steps, int64_t ckpt, const int* gauges, int n_gauges,
+                                    int64_t obs, double* traces_host) {
+  std::string err = adjoint_init();
+  if (!err.empty()) return err;
+  AdjointState& a = *adj_;
+  a.free_tape();
+  const int64_t C = mesh_.C;
+  a.scheme = scheme;
+  a.n_steps = n_steps;
+  a.ckpt = ckpt;
+  a.obs = obs;
+  a.n_gauges = n_gauges;
+  const int64_t n_obs = obs > 0 ? n_steps / obs : 0;
+  if (cudaMalloc(&a.d_dt, (n_steps ? n_steps : 1) * sizeof(double)) != cudaSuccess) return "tape allocation failed";
+  if (cudaMalloc(&a.d_traces, (n_obs * n_gauges ? n_obs * n_gauges : 1) * sizeof(double)) != cudaSuccess)
+    return "tape allocation failed";
+  if (cudaMalloc(&a.d_gauges, (n_gauges ? n_gauges : 1) * sizeof(int)) != cudaSuccess) return "tape allocation failed";
+  cudaMemcpy(a.d_gauges, gauges, n_gauges * sizeof(int), cudaMemcpyHostToDevice);
+  for (int64_t n = 0; n < n_steps; ++n) {
+    if (n % ckpt == 0) {
+      double* cp = nullptr;
+      if (cudaMalloc(&cp, 3 * C * sizeof(double)) != cudaSuccess) return "checkpoint allocation failed";
+      a.checkpoints.push_back(cp);
+      for (int q = 0; q < 3; ++q)
+        cudaMemcpyAsync(cp + q * C, state(0, q), C * sizeof(double), cudaMemcpyDeviceToDevice, stream_);
+    }
+    cudaError_t e = step(scheme, 1);
+    if (e != cudaSuccess) return std::string("forward step: ") + cudaGetErrorString(e);
+    cudaMemcpyAsync(a.d_dt + n, work_.dt, sizeof(double), cudaMemcpyDeviceToDevice, stream_);
+    if (obs > 0 && (n + 1) % obs == 0 && n_gauges > 0) {
+      const int64_t j = (n + 1) / obs - 1;
+      k_gather_gauges<<<(n_gauges + 255) / 256, 256, 0, stream_>>>(state(0, 0), a.d_gauges, n_gauges,
+                                                                    a.d_traces + j * n_gauges);
+      ++launches_;
+    }
+  }
+  if (traces_host && n_obs * n_gauges > 0)
+    cudaMemcpyAsync(traces_host, a.d_traces, n_obs * n_gauges * sizeof(double), cudaMemcpyDeviceToHost, stream_);
+  cudaError_t e = cudaStreamSynchronize(stream_);
+  if (e != cudaSuccess) return std::string("taped forward run: ") + cudaGetErrorString(e);
+  a.taped = true;
+  return "";
+}
+
+std::string Engine::adjoint_dts(double* out_host) {
+  if (!adj_ || !adj_->taped) return "no taped forward run";
+  cudaError_t e = cudaMemcpy(out_host, adj_->d_dt, adj_->n_steps * sizeof(double), cudaMemcpyDeviceToHost);
+  return e == cudaSuccess ? "" : cudaGetErrorString(e);
+}
+
+__global__ void k_interleave(const double* W, int C, double* out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < C) {
+    out[3 * i] = W[i];
+    out[3 * i + 1] = W[C + i];
+    out[3 * i + 2] = W[2 * C + i];
+  }
+}
+
+std::string Engine::adjoint_backward(const double* trace_grads_host, double* grad_prim_host, double* grad_z_host) {
+  if (!adj_ || !adj_->taped) return "no taped forward run to differentiate";
+  AdjointState& a = *adj_;
+  AdjWork& w = a.aw;
+  const int64_t C = mesh_.C, N = mesh_.N;
+  const Scheme sc = scheme_table(a.scheme);
+  const int ns = sc.n;
+  const int64_t n_obs = a.obs > 0 ? a.n_steps / a.obs : 0;
+  double* d_tg = nullptr;
+  if (cudaMalloc(&d_tg, (n_obs * a.n_gauges ? n_obs * a.n_gauges : 1) * sizeof(double)) != cudaSuccess)
+    return "allocation failed";
+  if (n_obs * a.n_gauges)
+    cudaMemcpy(d_tg, trace_grads_host, n_obs * a.n_gauges * sizeof(double), cudaMemcpyHostToDevice);
+  // stage-input store of one segment: [K][ns] states of 3C, plus the segment end
+  const int64_t K = a.ckpt;
+  std::vector<double*> store((size_t)K * ns + 1, nullptr);
+  for (auto& p : store)
+    if (cudaMalloc(&p, 3 * C * sizeof(double)) != cudaSuccess) {
+      cudaFree(d_tg);
+      for (auto& q : store)
+        if (q) cudaFree(q);
+      return "segment store allocation failed";
+    }
+  double* lam_cur = w.lam;
+  cudaMemsetAsync(w.lam, 0, 3 * C * sizeof(double), stream_);
+  cudaMemsetAsync(w.lz, 0, N * sizeof(double), stream_);
+  cudaMemsetAsync(w.lscatter, 0, C * sizeof(double), stream_);
+  double tsum_saved = 0.;  // the recompute must not advance the context's clock
+  cudaMemcpyAsync(&tsum_saved, work_.tsum, sizeof(double), cudaMemcpyDeviceToHost, stream_);
+  cudaStreamSynchronize(stream_);
+  double* lam_step = nullptr;  // adjoint of the current step's end state
+  cudaMalloc(&lam_step, 3 * C * sizeof(double));
+  cudaMemsetAsync(lam_step, 0, 3 * C * sizeof(double), stream_);
+  const int b = 256, gc = (int)((C + b - 1) / b);
+  std::string err;
+  const int64_t nseg = (a.n_steps + K - 1) / K;
+  for (int64_t seg = nseg - 1; seg >= 0 && err.empty(); --seg) {
+    const int64_t s0 = seg * K, s1 = std::min(a.n_steps, s0 + K);
+    // recompute the segment stage by stage with the recorded dt
+    for (int q = 0; q < 3; ++q)
+      cudaMemcpyAsync(store[0] + q * C, a.checkpoints[seg] + q * C, C * sizeof(double), cudaMemcpyDeviceToDevice,
+                      stream_);
+    for (int64_t n = s0; n < s1; ++n) {
+      const int64_t base = (n - s0) * ns;
+      cudaMemcpyAsync(d_fixed_dt, a.d_dt + n, sizeof(double), cudaMemcpyDeviceToDevice, stream_);
+      double* S0p = store[base];
+      const double* u0[3] = {S0p, S0p + C, S0p + 2 * C};
+      for (int s = 0; s < ns; ++s) {
+        double* inp = store[base + s];
+        double* outp = store[base + s + 1];
+        const double* in[3] = {inp, inp + C, inp + 2 * C};
+        double* out[3] = {outp, outp + C, outp + 2 * C};
+        cudaError_t e = reset_pass();
+        if (e == cudaSuccess) e = launch_stage(sc.s[s], in, u0, out, s == 0, s == 0 ? 2 : 0);
+        if (e != cudaSuccess) {
+          err = std::string("segment recompute: ") + cudaGetErrorString(e);
+          break;
+        }
+      }
+      if (!err.empty()) break;
+    }
+    if (!err.empty()) break;
+    // reverse the steps of the segment
+    for (int64_t n = s1 - 1; n >= s0; --n) {
+      const int64_t base = (n - s0) * ns;
+      if (a.obs > 0 && (n + 1) % a.obs == 0 && a.n_gauges > 0) {
+        const int64_t j = (n + 1) / a.obs - 1;
+        k_seed_gauges<<<(a.n_gauges + 255) / 256, 256, 0, stream_>>>(lam_step, a.d_gauges, a.n_gauges,
+                                                                     d_tg + j * a.n_gauges);
+      }
+      cudaMemcpyAsync(work_.dt, a.d_dt + n, sizeof(double), cudaMemcpyDeviceToDevice, stream_);
+      double* S0p = store[base];
+      const double* u0[3] = {S0p, S0p + C, S0p + 2 * C};
+      cudaMemsetAsync(w.lam0, 0, 3 * C * sizeof(double), stream_);
+      cudaMemcpyAsync(w.lam, lam_step, 3 * C * sizeof(double), cudaMemcpyDeviceToDevice, stream_);
+      for (int s = ns - 1; s >= 0; --s) {
+        double* inp = store[base + s];
+        const double* in[3] = {inp, inp + C, inp + 2 * C};
+        cudaMemsetAsync(w.lamp, 0, 3 * C * sizeof(double), stream_);
+        cudaError_t e = adjoint_stage_reverse(sc.s[s], in, u0, w);
+        if (e != cudaSuccess) {
+          err = std::string("stage reverse: ") + cudaGetErrorString(e);
+          break;
+        }
+        k_fold_scatter<<<gc, b, 0, stream_>>>((int)C, w.lamp, w.lscatter);
+        cudaMemcpyAsync(w.lam, w.lamp, 3 * C * sizeof(double), cudaMemcpyDeviceToDevice, stream_);
+      }
+      if (!err.empty()) break;
+      // adjoint of the step's initial state: through the first stage's input and the Shu-Osher terms
+      k_add3<<<gc, b, 0, stream_>>>((int)C, w.lam, w.lam0, lam_step);
+    }
+  }
+  (void)lam_cur;
+  if (err.empty()) {
+    double* d_out = store[0];
+    k_interleave<<<gc, b, 0, stream_>>>(lam_step, (int)C, d_out);
+    cudaMemcpyAsync(grad_prim_host, d_out, 3 * C * sizeof(double), cudaMemcpyDeviceToHost, stream_);
+    cudaMemcpyAsync(grad_z_host, w.lz, N * sizeof(double), cudaMemcpyDeviceToHost, stream_);
+    cudaError_t e = cudaStreamSynchronize(stream_);
+    if (e != cudaSuccess) err = std::string("adjoint: ") + cudaGetErrorString(e);
+  }
+  cudaMemcpy(work_.tsum, &tsum_saved, sizeof(double), cudaMemcpyHostToDevice);
+  for (auto& p : store) cudaFree(p);
+  cudaFree(d_tg);
+  cudaFree(lam_step);
+  return err;
+}
+
+cudaError_t Engine::adjoint_stage_reverse(const Stage& st, const double* const* in, const double* const* u0,
+                                          AdjWork& aw) {
+  const int b = 256;
+  const int gc = (mesh_.C + b - 1) / b, ge = (mesh_.E + b - 1) / b;
+  // recompute the stage's forward intermediates from its input
+  cudaError_t e = reset_pass();
+  if (e == cudaSuccess) e = interface_values(in[0], in[1], in[2], 0);
+  if (e == cudaSuccess) e = fluxes(in[0]);
+  if (e != cudaSuccess) return e;
+  k_drain_keep<<<gc, b, 0, stream_>>>(mesh_, work_, in[0]);
+  k_adj_update<<<gc, b, 0, stream_>>>(mesh_, work_, aw, in[0], in[1], in[2], u0[0], u0[1], u0[2], st, batched_);
+  k_adj_drain<<<gc, b, 0, stream_>>>(mesh_, work_, aw, in[0]);
+  switch (flux_ * 3 + ws_) {
+    case 0: k_adj_flux<0, 0><<<ge, b, 0, stream_>>>(mesh_, work_, aw, in[0]); break;
+    case 1: k_adj_flux<0, 1><<<ge, b, 0, stream_>>>(mesh_, work_, aw, in[0]); break;
+    case 2: k_adj_flux<0, 2><<<ge, b, 0, stream_>>>(mesh_, work_, aw, in[0]); break;
+    case 3: k_adj_flux<1, 0><<<ge, b, 0, stream_>>>(mesh_, work_, aw, in[0]); break;
+    case 4: k_adj_flux<1, 1><<<ge, b, 0, stream_>>>(mesh_, work_, aw, in[0]); break;
+    default: k_adj_flux<1, 2><<<ge, b, 0, stream_>>>(mesh_, work_, aw, in[0]); break;
+  }
+  k_adj_recon<<<gc, b, 0, stream_>>>(mesh_, work_, aw, in[0], in[1], in[2], batched_);
+  launches_ += 5;
+  return cudaGetLastError();
+}
+
+}  // namespace swe

@@ -38,6 +38,8 @@ struct Pw2Rec {
   double dedge[3][2]; // E_k - T, cell edge order
   int lo;             // global id of the lowest node
   int flat;           // b13 - b23 < tol
+  int sk[3];          // local (cell-order) index of each sorted vertex
+  int pad;
 };
 
 struct DevMesh {
@@ -121,6 +123,10 @@ struct HostInstance {
   double cfl, cor;
 };
 
+struct AdjWork;
+struct AdjointState;
+void adjoint_state_delete(AdjointState* a);
+
 class Engine {
  public:
   Engine() = default;
@@ -148,6 +154,25 @@ class Engine {
   // adds the durations (ms) of k_recon1, k_recon2, k_flux, k_drain, k_update
   // to acc[0..4] and the whole step to acc[5].  Synchronises.
   cudaError_t step_timed(int scheme, int latch_mode, double* acc);
+
+  // Discrete adjoint (swe_adjoint.cu): reverse of one stage whose input is
+  // `in` and whose step started from `u0`, given aw.lam; accumulates aw.lamp,
+  // aw.lam0, aw.lz.
+  cudaError_t adjoint_stage_reverse(const Stage& st, const double* const* in, const double* const* u0, AdjWork& aw);
+  // Taped forward run for the adjoint: n_steps CFL steps from the current
+  // state, checkpoint every ckpt steps, w at the gauge cells every obs steps
+  // into traces_host (n_steps / obs rows).  Returns "" or an error message.
+  std::string adjoint_init();
+  std::string adjoint_forward(int scheme, int64_t n_steps, int64_t ckpt, const int* gauges, int n_gauges,
+                              int64_t obs, double* traces_host);
+  // Reverse of the taped run: trace_grads (n_obs x n_gauges) are the adjoints
+  // of the traces; returns the gradient with respect to the initial primitive
+  // state (3 x C interleaved) and the node bathymetry (N).
+  std::string adjoint_backward(const double* trace_grads_host, double* grad_prim_host, double* grad_z_host);
+  std::string adjoint_dts(double* out_host);
+  // Runs `in` -> `out` for one stage with the engine's current dt (no latch).
+  cudaError_t stage_explicit(const Stage& st, const double* const* in, const double* const* u0, double* const* out,
+                             int latch_mode);
 
   int C() const { return mesh_.C; }
   int E() const { return mesh_.E; }
@@ -184,6 +209,7 @@ class Engine {
   bool batched_ = false;
   int64_t launches_ = 0;
   cudaGraphExec_t graphs_[3][3] = {};
+  AdjointState* adj_ = nullptr;
 };
 
 // Precompute (swe_precompute.cu): fills the host images of DevMesh arrays for

@@ -476,6 +476,7 @@ T* Engine::dalloc(size_t n) {
 }
 
 Engine::~Engine() {
+  if (adj_) adjoint_state_delete(adj_);
   for (auto& row : graphs_)
     for (auto& g : row)
       if (g) cudaGraphExecDestroy(g);
@@ -709,6 +710,11 @@ cudaError_t Engine::step_timed(int scheme, int latch_mode, double* acc) {
   for (auto& row : ev)
     for (auto& x : row) cudaEventDestroy(x);
   return e;
+}
+
+cudaError_t Engine::stage_explicit(const Stage& st, const double* const* in, const double* const* u0,
+                                   double* const* out, int latch_mode) {
+  return launch_stage(st, in, u0, out, true, latch_mode);
 }
 
 cudaError_t Engine::step(int scheme, int latch_mode) {

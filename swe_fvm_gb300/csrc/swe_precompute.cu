@@ -284,6 +284,10 @@ void precompute_instance(const HostInstance& h, int inst, int64_t c0, int64_t e0
           q.dedge[k][1] = Ek[k][1] - ti[1];
         }
         q.lo = (int)(n0 + sp[0]);
+        for (int s2 = 0; s2 < 3; ++s2)
+          for (int k = 0; k < 3; ++k)
+            if (ip[k] == sp[s2]) q.sk[s2] = k;
+        q.pad = 0;
       }
     }
   };
