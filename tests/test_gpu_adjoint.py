@@ -84,8 +84,17 @@ def test_gradient_initial_surface_matches_central_differences(gpu, adjoint_run):
 
 
 def test_gradient_bathymetry_matches_central_differences(gpu, adjoint_run):
+    """At nodes whose surrounding cells are all wet: at a node touching a dry
+    cell (level exactly at the cell bathymetry) the loss has a kink, a one-sided
+    perturbation turns the cell wet, and central differences are meaningless."""
     m, prim, gauges, traces, target, dts, gp, gz = adjoint_run
-    cand = np.argsort(-np.abs(gz))[:6]
+    h = prim[:, 0] - m.centroids()[:, 2]
+    node_min_h = np.full(m.num_nodes, np.inf)
+    np.minimum.at(node_min_h, m.cell_nodes.reshape(-1), np.repeat(h, 3))
+    boundary = np.zeros(m.num_nodes, bool)
+    boundary[m.edge_nodes[m.edge_cells[:, 1] < 0].reshape(-1)] = True
+    ok = np.where((node_min_h > 0.02) & ~boundary)[0]
+    cand = ok[np.argsort(-np.abs(gz[ok]))[:6]]
     eps = 1e-7
     errs = []
     for nd in cand:
