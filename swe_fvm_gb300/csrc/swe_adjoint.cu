@@ -502,6 +502,39 @@ __device__ void slot_reverse(double ze, double a_w, double u0, double v0, double
   *lze = lz;
 }
 
+// The fully-wet plane of cell c for neighbour combination `mask`: slope as a
+// Dual<3> over the z of its three points (neighbour centroid, or edge centre
+// where the neighbour is partially wet), coordinates relative to c's centroid.
+__device__ void combo_plane_dual(const DevMesh& m, int c, int mask, Dual<3>* g0, Dual<3>* g1) {
+  typedef Dual<3> D;
+  const int C = m.C;
+  const Pw2Rec& r = m.pw2[c];
+  D pz[3];
+  double px[3], py[3];
+  for (int k = 0; k < 3; ++k) {
+    const int nb = m.cnbr[k * C + c];
+    if ((mask >> k) & 1) {
+      pz[k] = D::var(m.ze[k * C + c], k);
+      px[k] = r.dedge[k][0];
+      py[k] = r.dedge[k][1];
+    } else {
+      pz[k] = D::var(m.bc[nb], k);
+      const Pw2Rec& rn = m.pw2[nb];
+      px[k] = (rn.p[0][0] + rn.tp0x) - (r.p[0][0] + r.tp0x);
+      py[k] = (rn.p[0][1] + rn.tp0y) - (r.p[0][1] + r.tp0y);
+    }
+  }
+  plane_gradient_t(D(px[0]), D(py[0]), pz[0], D(px[1]), D(py[1]), pz[1], D(px[2]), D(py[2]), pz[2], g0, g1);
+}
+// adjoint lp[k] of the plane's point z -> node bathymetry
+__device__ void combo_points_to_nodes(const DevMesh& m, AdjWork& aw, int c, int mask, const double* lp) {
+  for (int k = 0; k < 3; ++k) {
+    if (lp[k] == 0.) continue;
+    if ((mask >> k) & 1) lam_edge_z(m, aw, c, k, lp[k]);
+    else lam_cell_z(m, aw, m.cnbr[k * m.C + c], lp[k]);
+  }
+}
+
 __global__ void __launch_bounds__(256) k_adj_recon(DevMesh m, DevWork wk, AdjWork aw, const double* W,
                                                    const double* U, const double* V, int batched) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -602,38 +635,18 @@ __global__ void __launch_bounds__(256) k_adj_recon(DevMesh m, DevWork wk, AdjWor
     lw_i += lw0;
     if (p.kept) {
       // the combination plane through neighbour centroids / edge centres
-      typedef Dual<3> D;
-      D pz[3];
-      double px[3], py[3];
       const Pw2Rec& r = m.pw2[i];
-      for (int k = 0; k < 3; ++k) {
-        const int nb = m.cnbr[k * C + i];
-        if ((p.mask >> k) & 1) {
-          pz[k] = D::var(m.ze[k * C + i], k);
-          px[k] = r.dedge[k][0];
-          py[k] = r.dedge[k][1];
-        } else {
-          pz[k] = D::var(m.bc[nb], k);
-          // neighbour centroid relative to this cell's centroid
-          const Pw2Rec& rn = m.pw2[nb];
-          px[k] = (rn.p[0][0] + rn.tp0x) - (r.p[0][0] + r.tp0x);
-          py[k] = (rn.p[0][1] + rn.tp0y) - (r.p[0][1] + r.tp0y);
-        }
-      }
-      D g0, g1;
-      plane_gradient_t(D(px[0]), D(py[0]), pz[0], D(px[1]), D(py[1]), pz[1], D(px[2]), D(py[2]), pz[2], &g0, &g1);
+      Dual<3> g0, g1;
+      combo_plane_dual(m, i, p.mask, &g0, &g1);
       // off_k = g0 dEx + g1 dEy
       double lg0 = lgx, lg1 = lgy;
       for (int k = 0; k < 3; ++k) {
         lg0 += loff[k] * r.dedge[k][0];
         lg1 += loff[k] * r.dedge[k][1];
       }
-      for (int k = 0; k < 3; ++k) {
-        const double lp = lg0 * g0.d[k] + lg1 * g1.d[k];
-        if (lp == 0.) continue;
-        if ((p.mask >> k) & 1) lam_edge_z(m, aw, i, k, lp);
-        else lam_cell_z(m, aw, m.cnbr[k * C + i], lp);
-      }
+      double lp[3];
+      for (int k = 0; k < 3; ++k) lp[k] = lg0 * g0.d[k] + lg1 * g1.d[k];
+      combo_points_to_nodes(m, aw, i, p.mask, lp);
     }
   } else {
     const Pw2Rec& r = m.pw2[i];
@@ -701,7 +714,17 @@ __global__ void __launch_bounds__(256) k_adj_recon(DevMesh m, DevWork wk, AdjWor
             if (!dge0(a - zc_)) {
               atomicAdd(aw.lz + cnode(m, best, bestk), g[1]);
             } else if (pc.type == 2) {
-              atomicAdd(aw.lscatter + best, g[1]);  // w of a fully-wet cell (+ bathymetry offset, not tracked)
+              atomicAdd(aw.lscatter + best, g[1]);  // the fully-wet cell's level
+              if (pc.kept) {
+                // its vertex offset a_k = g . (P_k - T) moves with the plane's point z
+                Dual<3> g0, g1;
+                combo_plane_dual(m, best, pc.mask, &g0, &g1);
+                const Pw2Rec& rb = m.pw2[best];
+                double lp[3];
+                for (int q = 0; q < 3; ++q)
+                  lp[q] = g[1] * (g0.d[q] * rb.dnode[bestk][0] + g1.d[q] * rb.dnode[bestk][1]);
+                combo_points_to_nodes(m, aw, best, pc.mask, lp);
+              }
             } else {
               typedef Dual<4> F4;
               F4 wb = F4::var(W[best], 0);
