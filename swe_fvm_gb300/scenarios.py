@@ -142,6 +142,26 @@ def hump_instance(seed: int, cells: int):
     return mesh, prim
 
 
+def sloped_bump_case(lattice: int = 25, seed: int = 9):
+    """Jittered-lattice Delaunay mesh of the unit square over a bed that is
+    sloped everywhere (a tilt plus one broad bump that emerges), a Gaussian
+    hump and a background current: no flat regions, so the binary limiter and
+    the HLLC star-velocity switch are away from their kinks except at the
+    wet/dry front (used by the adjoint's finite-difference checks)."""
+    xyz, tri = jittered_delaunay(lattice, seed)
+    x, y = xyz[:, 0], xyz[:, 1]
+    xyz[:, 2] = 0.08 * x + 0.05 * y + 0.25 * np.exp(-((x - 0.7) ** 2 + (y - 0.35) ** 2) / (2 * 0.12 ** 2))
+    mesh = build_topology(xyz, tri)
+    cen = mesh.centroids()
+    w0 = 0.2 + 0.04 * np.exp(-((cen[:, 0] - 0.3) ** 2 + (cen[:, 1] - 0.6) ** 2) / (2 * 0.1 ** 2))
+    prim = np.zeros((mesh.num_cells, 3))
+    prim[:, 0] = np.maximum(w0, cen[:, 2])
+    wet = prim[:, 0] - cen[:, 2] > 1e-12
+    prim[wet, 1] = 0.05
+    prim[wet, 2] = 0.03
+    return mesh, prim
+
+
 def ensemble_sizes(n_instances: int = 256, lo: int = 2000, hi: int = 200000, seed: int = 7):
     """Cell counts log-uniform in [lo, hi]."""
     rng = np.random.default_rng(seed)

@@ -16,14 +16,10 @@ N_STEPS, OBS, CKPT = 24, 4, 10
 
 
 def case():
-    """The ensemble's hump over bumps, with a background current so that no
-    interface sits at the HLLC star-velocity switch u* = 0 (still water puts
-    every edge exactly on it: the flux is only piecewise smooth there and the
-    adjoint returns the derivative of the branch the forward took)."""
-    m, prim = scenarios.hump_instance(4242, 1200)
-    wet = prim[:, 0] - m.centroids()[:, 2] > 1e-12
-    prim[wet, 1] = 0.05
-    prim[wet, 2] = 0.03
+    """A bed sloped everywhere with an emerging bump, a hump and a current
+    (scenarios.sloped_bump_case): the finite differences are taken where no
+    limiter, wet/dry or HLLC branch switch is within reach of the step."""
+    m, prim = scenarios.sloped_bump_case(25, 9)
     rng = np.random.default_rng(5)
     gauges = rng.choice(m.num_cells, 12, replace=False)
     return m.contiguous(), prim, gauges
