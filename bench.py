@@ -234,6 +234,8 @@ def run_gpu(args):
     }
     if ENSEMBLE_INSTANCES > 0 and not args.no_ensemble:
         out["batched"] = run_ensemble(torch, stream)
+    if ADJ_STEPS > 0 and not args.no_adjoint:
+        out["adjoint"] = run_adjoint(torch, stream)
     if rank == 0:
         if world == 1 and not args.no_cpu:
             out["cpu_baseline"] = cpu_baseline(mesh, prim)
@@ -302,6 +304,67 @@ def run_ensemble(torch, stream):
                        "flux": "HLLC+Einfeldt", "scheme": "SSPRK2", "mesh_gen_s": round(t_gen, 1)}}
 
 
+ADJ_CELLS = int(os.environ.get("SWE_BENCH_ADJ_CELLS", "250000"))
+ADJ_STEPS = int(os.environ.get("SWE_BENCH_ADJ_STEPS", "2000"))
+
+
+def run_adjoint(torch, stream):
+    """Adjoint config: 250k-cell seeded Delaunay mesh, bump bathymetry, hump
+    surface, SSPRK2 (HLLC + Einfeldt, CFL 0.15), 2000 steps, 64 random gauge
+    cells observed every 10th step, checkpoint every 50 steps; target traces
+    from a run whose bathymetry carries 5% seeded Gaussian noise.  Reports the
+    cost ratio (taped forward + backward) / plain forward solve and runs the
+    loss gradient once through the torch.autograd.Function."""
+    from swe_fvm_gb300 import Fluxes, SpaceDisc, Wavespeeds, scenarios
+    from swe_fvm_gb300.adjoint import Rollout, gauge_rollout
+    from swe_fvm_gb300.mesh import Mesh
+
+    mesh, prim = scenarios.hump_instance(2024, ADJ_CELLS)
+    mesh = mesh.contiguous()
+    rng = np.random.default_rng(11)
+    gauges = rng.choice(mesh.num_cells, 64, replace=False)
+    obs, ckpt = 10, 50
+    g = mesh.geometry.copy()
+    g[:, 2] = g[:, 2] * (1.0 + 0.05 * rng.standard_normal(mesh.num_nodes))
+    noisy = Mesh(g, mesh.edge_nodes, mesh.edge_cells, mesh.cell_nodes, mesh.cell_edges, mesh.cell_neighbours)
+    target = Rollout(noisy, prim).forward(1, ADJ_STEPS, ckpt, gauges, obs)
+    fl = Fluxes.HLLC(Wavespeeds.Einfeldt)
+    # plain forward solve
+    sd = SpaceDisc(fl, mesh, prim)
+    sd.set_stream(stream.cuda_stream)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    sd.run_cfl(1, ADJ_STEPS)
+    sd.synchronize()
+    t_plain = time.perf_counter() - t0
+    del sd
+    # taped forward + backward through the C ABI
+    ro = Rollout(mesh, prim)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    traces = ro.forward(1, ADJ_STEPS, ckpt, gauges, obs)
+    t_fwd = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    gp, gz = ro.backward(2.0 * (traces - target))
+    t_bwd = time.perf_counter() - t0
+    loss = float(np.sum((traces - target) ** 2))
+    # the same gradient through torch.autograd
+    w0 = torch.tensor(prim[:, 0], dtype=torch.float64, device="cuda", requires_grad=True)
+    z = torch.tensor(mesh.geometry[:, 2], dtype=torch.float64, device="cuda", requires_grad=True)
+    tr = gauge_rollout(w0, z, mesh, gauges, ADJ_STEPS, obs, ckpt, uv0=prim[:, 1:])
+    lt = ((tr - torch.from_numpy(target).cuda()) ** 2).sum()
+    lt.backward()
+    agree = bool(np.allclose(w0.grad.cpu().numpy(), gp[:, 0], rtol=1e-12, atol=0) and
+                 np.allclose(z.grad.cpu().numpy(), gz, rtol=1e-9, atol=1e-300))
+    return {"metric": "adjoint/forward time ratio (taped forward + backward) / plain forward",
+            "ratio": (t_fwd + t_bwd) / t_plain, "higher_is_better": False, "plain_forward_s": t_plain,
+            "taped_forward_s": t_fwd, "backward_s": t_bwd, "cells": mesh.num_cells, "steps": ADJ_STEPS,
+            "gauges": 64, "obs_every": obs, "checkpoint_every": ckpt, "loss": loss,
+            "grad_norm_w0": float(np.linalg.norm(gp[:, 0])), "grad_norm_z": float(np.linalg.norm(gz)),
+            "autograd_matches_c_abi": agree,
+            "config": {"workload": "adjoint_250k", "flux": "HLLC+Einfeldt", "scheme": "SSPRK2", "cfl": 0.15}}
+
+
 # DRAM bytes per SSPRK2 step from the ncu launch capture (sum over the step's
 # 10 kernels); filled from the committed profile summary.
 TRAFFIC_PER_STEP = {}
@@ -353,6 +416,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--profile", action="store_true", help="only warm-up + K steps (for ncu captures)")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the batched-ensemble leg")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint leg")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

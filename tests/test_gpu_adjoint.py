@@ -111,3 +111,18 @@ def test_gradient_bathymetry_matches_central_differences(gpu, adjoint_run):
         errs.append(abs(gz[nd] - d) / max(abs(d), 1e-30))
     assert np.median(errs) < 1e-5, errs
     assert max(errs) < 1e-3, errs
+
+
+def test_autograd_function_matches_c_abi(gpu, adjoint_run):
+    torch = pytest.importorskip("torch")
+    from swe_fvm_gb300.adjoint import gauge_rollout
+
+    m, prim, gauges, traces, target, dts, gp, gz = adjoint_run
+    w0 = torch.tensor(prim[:, 0], dtype=torch.float64, device="cuda", requires_grad=True)
+    z = torch.tensor(m.geometry[:, 2], dtype=torch.float64, device="cuda", requires_grad=True)
+    tr = gauge_rollout(w0, z, m, gauges, N_STEPS, OBS, CKPT, uv0=prim[:, 1:], cfl=0.3)
+    assert np.array_equal(tr.detach().cpu().numpy(), traces)
+    loss = ((tr - torch.from_numpy(target).cuda()) ** 2).sum()
+    loss.backward()
+    assert np.allclose(w0.grad.cpu().numpy(), gp[:, 0], rtol=1e-12, atol=1e-300)
+    assert np.allclose(z.grad.cpu().numpy(), gz, rtol=1e-9, atol=1e-300)
