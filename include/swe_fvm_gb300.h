@@ -159,6 +159,12 @@ swe_status swe_measure_fp64_peak(double* tflops);
  * counterpart. */
 swe_status swe_selftest_fp64(int64_t n, uint64_t seed, int64_t* div_mismatches, int64_t* sqrt_mismatches);
 
+/* Compares the hand-written reverse of the flux plugin (flux, wavespeed) with
+ * its forward-mode Jacobian on n random interface states (some with a dry
+ * side) and returns the largest relative difference of the adjoint.  No
+ * reference counterpart. */
+swe_status swe_selftest_flux_adjoint(int32_t flux, int32_t wavespeed, int64_t n, uint64_t seed, double* max_rel_err);
+
 /* Size and counters. */
 swe_status swe_num_cells(swe_ctx* ctx, int64_t* n);
 /* Kernel launches issued so far by this context (all streams, graphs counted

@@ -29,7 +29,7 @@ EXPORTS = [
     "swe_params_default", "swe_create", "swe_destroy", "swe_set_stream", "swe_step", "swe_run", "swe_run_cfl",
     "swe_cfl_dt", "swe_min_len_to_wavespeed", "swe_compute_interface_values", "swe_compute_fluxes",
     "swe_get_prim", "swe_set_prim", "swe_get_prim_device", "swe_set_prim_device", "swe_get_edge_values",
-    "swe_get_fluxes", "swe_get_node_max", "swe_time_kernels", "swe_measure_fp64_peak", "swe_selftest_fp64", "swe_num_cells", "swe_launch_count", "swe_synchronize",
+    "swe_get_fluxes", "swe_get_node_max", "swe_time_kernels", "swe_measure_fp64_peak", "swe_selftest_fp64", "swe_selftest_flux_adjoint", "swe_num_cells", "swe_launch_count", "swe_synchronize",
     "swe_last_error", "swe_adjoint_forward", "swe_adjoint_backward", "swe_adjoint_dts", "swe_edge_fluxes_noalloc", "swe_batch_create", "swe_batch_destroy", "swe_batch_set_stream", "swe_batch_run_cfl", "swe_batch_run",
     "swe_batch_get_prim", "swe_batch_time", "swe_batch_launch_count", "swe_batch_synchronize",
     "swe_batch_last_error",
@@ -107,6 +107,7 @@ def load(build_if_needed: bool = True):
         "swe_time_kernels": [vp, i32, i64, vp],
         "swe_measure_fp64_peak": [P(d)],
         "swe_selftest_fp64": [i64, ctypes.c_uint64, P(i64), P(i64)],
+        "swe_selftest_flux_adjoint": [i32, i32, i64, ctypes.c_uint64, P(d)],
         "swe_num_cells": [vp, P(i64)],
         "swe_launch_count": [vp, P(i64)],
         "swe_synchronize": [vp],

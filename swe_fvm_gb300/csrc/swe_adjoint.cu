@@ -26,6 +26,7 @@
 
 #include "swe_adjoint.cuh"
 #include "swe_dual.cuh"
+#include "swe_flux_adjoint.cuh"
 
 namespace swe {
 
@@ -281,22 +282,24 @@ __global__ void __launch_bounds__(256) k_adj_flux(DevMesh m, DevWork wk, AdjWork
   lF[1] += aw.lF1[sr];
   lF[2] += aw.lF2[sr];
   if (lF[0] == 0. && lF[1] == 0. && lF[2] == 0.) return;
-  typedef Dual<7> D;
-  D Lw = D::var(wk.ew[sl], 0), Lu = D::var(wk.eu[sl], 1), Lv = D::var(wk.ev[sl], 2);
-  D Rw = D::var(wk.ew[sr], 3), Ru = D::var(wk.eu[sr], 4), Rv = D::var(wk.ev[sr], 5);
-  D b = D::var(m.ezm[e], 6);
-  D F[3];
-  flux_t(FLUX, WS, nx, ny, m.etx[e], m.ety[e], b, Lw, Lu, Lv, Rw, Ru, Rv, F);
-  double g[7];
-#pragma unroll
-  for (int k = 0; k < 7; ++k) g[k] = lF[0] * F[0].d[k] + lF[1] * F[1].d[k] + lF[2] * F[2].d[k];
-  aw.lew[sl] += g[0];
-  aw.leu[sl] += g[1];
-  aw.lev[sl] += g[2];
-  aw.lew[sr] += g[3];
-  aw.leu[sr] += g[4];
-  aw.lev[sr] += g[5];
-  aw.lze[sl] += g[6];
+  EdgeGeom g;
+  g.nx = nx;
+  g.ny = ny;
+  g.tx = m.etx[e];
+  g.ty = m.ety[e];
+  g.b = m.ezm[e];
+  g.lmin = m.elmin[e];
+  SideState L{wk.ew[sl], wk.eu[sl], wk.ev[sl]};
+  SideState R{wk.ew[sr], wk.eu[sr], wk.ev[sr]};
+  double lL[3] = {0., 0., 0.}, lR[3] = {0., 0., 0.}, lb = 0.;
+  flux_reverse(FLUX, WS, g, L, R, lF, lL, lR, &lb);
+  aw.lew[sl] += lL[0];
+  aw.leu[sl] += lL[1];
+  aw.lev[sl] += lL[2];
+  aw.lew[sr] += lR[0];
+  aw.leu[sr] += lR[1];
+  aw.lev[sr] += lR[2];
+  aw.lze[sl] += lb;
 }
 
 // ------------------------------------------------------- R4: reconstruction
@@ -502,29 +505,36 @@ __device__ void slot_reverse(double ze, double a_w, double u0, double v0, double
   *lze = lz;
 }
 
-// The fully-wet plane of cell c for neighbour combination `mask`: slope as a
-// Dual<3> over the z of its three points (neighbour centroid, or edge centre
-// where the neighbour is partially wet), coordinates relative to c's centroid.
-__device__ void combo_plane_dual(const DevMesh& m, int c, int mask, Dual<3>* g0, Dual<3>* g1) {
-  typedef Dual<3> D;
+// Adjoint of the z of the three points of a plane slope (plane_gradient):
+// with M = [[x1-x0, y1-y0], [x2-x0, y2-y0]] the slope is M^-1 (z1-z0, z2-z0),
+// so (lz1, lz2) = M^-T (lg0, lg1) and lz0 = -(lz1 + lz2).
+__device__ void plane_points_adjoint(const double* px, const double* py, double lg0, double lg1, double* lp) {
+  const double a00 = px[1] - px[0], a01 = py[1] - py[0];
+  const double a10 = px[2] - px[0], a11 = py[2] - py[0];
+  const double det = a00 * a11 - a01 * a10;
+  const double l1 = SWE_DIV(lg0 * a11 - lg1 * a10, det);
+  const double l2 = SWE_DIV(-lg0 * a01 + lg1 * a00, det);
+  lp[0] = -(l1 + l2);
+  lp[1] = l1;
+  lp[2] = l2;
+}
+// points of the fully-wet plane of cell c for neighbour combination `mask`
+// (neighbour centroid, or edge centre where the neighbour is partially wet),
+// relative to c's centroid
+__device__ void combo_plane_points(const DevMesh& m, int c, int mask, double* px, double* py) {
   const int C = m.C;
   const Pw2Rec& r = m.pw2[c];
-  D pz[3];
-  double px[3], py[3];
   for (int k = 0; k < 3; ++k) {
     const int nb = m.cnbr[k * C + c];
     if ((mask >> k) & 1) {
-      pz[k] = D::var(m.ze[k * C + c], k);
       px[k] = r.dedge[k][0];
       py[k] = r.dedge[k][1];
     } else {
-      pz[k] = D::var(m.bc[nb], k);
       const Pw2Rec& rn = m.pw2[nb];
       px[k] = (rn.p[0][0] + rn.tp0x) - (r.p[0][0] + r.tp0x);
       py[k] = (rn.p[0][1] + rn.tp0y) - (r.p[0][1] + r.tp0y);
     }
   }
-  plane_gradient_t(D(px[0]), D(py[0]), pz[0], D(px[1]), D(py[1]), pz[1], D(px[2]), D(py[2]), pz[2], g0, g1);
 }
 // adjoint lp[k] of the plane's point z -> node bathymetry
 __device__ void combo_points_to_nodes(const DevMesh& m, AdjWork& aw, int c, int mask, const double* lp) {
@@ -636,16 +646,15 @@ __global__ void __launch_bounds__(256) k_adj_recon(DevMesh m, DevWork wk, AdjWor
     if (p.kept) {
       // the combination plane through neighbour centroids / edge centres
       const Pw2Rec& r = m.pw2[i];
-      Dual<3> g0, g1;
-      combo_plane_dual(m, i, p.mask, &g0, &g1);
       // off_k = g0 dEx + g1 dEy
       double lg0 = lgx, lg1 = lgy;
       for (int k = 0; k < 3; ++k) {
         lg0 += loff[k] * r.dedge[k][0];
         lg1 += loff[k] * r.dedge[k][1];
       }
-      double lp[3];
-      for (int k = 0; k < 3; ++k) lp[k] = lg0 * g0.d[k] + lg1 * g1.d[k];
+      double px[3], py[3], lp[3];
+      combo_plane_points(m, i, p.mask, px, py);
+      plane_points_adjoint(px, py, lg0, lg1, lp);
       combo_points_to_nodes(m, aw, i, p.mask, lp);
     }
   } else {
@@ -717,12 +726,10 @@ __global__ void __launch_bounds__(256) k_adj_recon(DevMesh m, DevWork wk, AdjWor
               atomicAdd(aw.lscatter + best, g[1]);  // the fully-wet cell's level
               if (pc.kept) {
                 // its vertex offset a_k = g . (P_k - T) moves with the plane's point z
-                Dual<3> g0, g1;
-                combo_plane_dual(m, best, pc.mask, &g0, &g1);
                 const Pw2Rec& rb = m.pw2[best];
-                double lp[3];
-                for (int q = 0; q < 3; ++q)
-                  lp[q] = g[1] * (g0.d[q] * rb.dnode[bestk][0] + g1.d[q] * rb.dnode[bestk][1]);
+                double px[3], py[3], lp[3];
+                combo_plane_points(m, best, pc.mask, px, py);
+                plane_points_adjoint(px, py, g[1] * rb.dnode[bestk][0], g[1] * rb.dnode[bestk][1], lp);
                 combo_points_to_nodes(m, aw, best, pc.mask, lp);
               }
             } else {

@@ -60,6 +60,8 @@ extern "C" swe_status swe_measure_fp64_peak(double* tflops) {
 // against the hardware instructions on n pseudo-random operand pairs.
 
 #include "swe_fp64.cuh"
+#include "swe_dual.cuh"
+#include "swe_flux_adjoint.cuh"
 
 namespace {
 
@@ -125,4 +127,61 @@ extern "C" swe_status swe_selftest_fp64(int64_t n, uint64_t seed, int64_t* div_m
   *div_mismatches = (int64_t)h[0];
   *sqrt_mismatches = (int64_t)h[1];
   return SWE_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Self-test of the hand-written flux reverse against the forward-mode
+// Jacobian (Dual<7>) on random interface states.
+namespace {
+
+__global__ void k_flux_adj_selftest(int flux, int ws, int n, unsigned long long seed, double* maxerr) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  auto U = [&](int k) {
+    return (double)(splitmix(seed ^ (16ull * i + k)) >> 11) * (1.0 / 9007199254740992.0);
+  };
+  const double ang = 6.283185307179586 * U(0);
+  swe::EdgeGeom g;
+  g.nx = cos(ang);
+  g.ny = sin(ang);
+  g.tx = -g.ny;
+  g.ty = g.nx;
+  g.b = 0.3 * U(1) - 0.1;
+  g.lmin = 0.01;
+  const int dry = (int)(U(2) * 8.0);  // sometimes a dry side
+  swe::SideState L{g.b + (dry == 0 ? 0. : 0.01 + 0.5 * U(3)), U(4) - 0.5, U(5) - 0.5};
+  swe::SideState R{g.b + (dry == 1 ? 0. : 0.01 + 0.5 * U(6)), U(7) - 0.5, U(8) - 0.5};
+  if (dry == 0) L.u = L.v = 0.;
+  if (dry == 1) R.u = R.v = 0.;
+  const double lF[3] = {U(9) - 0.5, U(10) - 0.5, U(11) - 0.5};
+  double lL[3] = {0., 0., 0.}, lR[3] = {0., 0., 0.}, lb = 0.;
+  swe::flux_reverse(flux, ws, g, L, R, lF, lL, lR, &lb);
+  typedef swe::Dual<7> D;
+  D F[3];
+  swe::flux_t(flux, ws, g.nx, g.ny, g.tx, g.ty, D::var(g.b, 6), D::var(L.w, 0), D::var(L.u, 1), D::var(L.v, 2),
+              D::var(R.w, 3), D::var(R.u, 4), D::var(R.v, 5), F);
+  const double hand[7] = {lL[0], lL[1], lL[2], lR[0], lR[1], lR[2], lb};
+  double err = 0.;
+  for (int k = 0; k < 7; ++k) {
+    const double ref = lF[0] * F[0].d[k] + lF[1] * F[1].d[k] + lF[2] * F[2].d[k];
+    const double e = fabs(hand[k] - ref) / (fabs(ref) + 1e-12);
+    if (e > err) err = e;
+  }
+  // exact max via integer atomics on the (non-negative) double bit pattern
+  atomicMax((unsigned long long*)maxerr, (unsigned long long)__double_as_longlong(err));
+}
+
+}  // namespace
+
+extern "C" swe_status swe_selftest_flux_adjoint(int32_t flux, int32_t wavespeed, int64_t n, uint64_t seed,
+                                                double* max_rel_err) {
+  if (!max_rel_err || n <= 0 || n > (1 << 26) || flux < 0 || flux > 1 || wavespeed < 0 || wavespeed > 2)
+    return SWE_ERR_INVALID_ARGUMENT;
+  double* d = nullptr;
+  if (cudaMalloc(&d, sizeof(double)) != cudaSuccess) return SWE_ERR_OUT_OF_MEMORY;
+  cudaMemset(d, 0, sizeof(double));
+  k_flux_adj_selftest<<<(int)((n + 255) / 256), 256>>>(flux, wavespeed, (int)n, seed, d);
+  cudaError_t e = cudaMemcpy(max_rel_err, d, sizeof(double), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  return e == cudaSuccess ? SWE_OK : SWE_ERR_CUDA;
 }

@@ -125,4 +125,17 @@ def test_autograd_function_matches_c_abi(gpu, adjoint_run):
     loss = ((tr - torch.from_numpy(target).cuda()) ** 2).sum()
     loss.backward()
     assert np.allclose(w0.grad.cpu().numpy(), gp[:, 0], rtol=1e-12, atol=1e-300)
-    assert np.allclose(z.grad.cpu().numpy(), gz, rtol=1e-9, atol=1e-300)
+    # the bathymetry gradient sums with atomics: equal up to the summation order
+    assert np.linalg.norm(z.grad.cpu().numpy() - gz) <= 1e-12 * np.linalg.norm(gz)
+
+
+@pytest.mark.parametrize("flux", [0, 1])
+@pytest.mark.parametrize("ws", [0, 1, 2])
+def test_hand_flux_reverse_equals_dual_jacobian(gpu, flux, ws):
+    import ctypes
+
+    from swe_fvm_gb300 import _lib
+
+    err = ctypes.c_double(-1.0)
+    assert _lib.load().swe_selftest_flux_adjoint(flux, ws, 1 << 20, 7, ctypes.byref(err)) == 0
+    assert err.value < 1e-9, err.value
