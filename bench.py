@@ -154,6 +154,17 @@ def run_gpu(args):
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
     sd.set_stream(stream.cuda_stream)
+    if args.adjoint_profile:
+        # profiling driver for the reverse kernels: a short taped run and its reverse
+        from swe_fvm_gb300.adjoint import Rollout
+
+        ro = Rollout(mesh, prim)
+        gauges = np.arange(0, C, max(1, C // 64))
+        tr = ro.forward(1, args.steps, 10, gauges, 5)
+        ro.backward(np.ones_like(tr))
+        torch.cuda.synchronize()
+        print(json.dumps({"adjoint_profile": True, "cells": C, "steps": args.steps}))
+        return
     if args.profile:
         # profiling driver: warm-up, then exactly K graph-replayed steps
         sd.run_cfl(1, args.warmup)
@@ -417,6 +428,7 @@ def main():
     ap.add_argument("--profile", action="store_true", help="only warm-up + K steps (for ncu captures)")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the batched-ensemble leg")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint leg")
+    ap.add_argument("--adjoint-profile", action="store_true", help="only a short taped run and its reverse")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -161,7 +161,8 @@ swe_status swe_selftest_fp64(int64_t n, uint64_t seed, int64_t* div_mismatches, 
 
 /* Compares the hand-written reverse of the flux plugin (flux, wavespeed) with
  * its forward-mode Jacobian on n random interface states (some with a dry
- * side) and returns the largest relative difference of the adjoint.  No
+ * side) and returns the largest normwise relative difference of the
+ * 7-component adjoint (max |hand - dual| / max |dual|).  No
  * reference counterpart. */
 swe_status swe_selftest_flux_adjoint(int32_t flux, int32_t wavespeed, int64_t n, uint64_t seed, double* max_rel_err);
 
