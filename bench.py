@@ -155,15 +155,34 @@ def run_gpu(args):
     torch.cuda.set_stream(stream)
     sd.set_stream(stream.cuda_stream)
     if args.adjoint_profile:
-        # profiling driver for the reverse kernels: a short taped run and its reverse
+        # profiling driver for the reverse kernels: the adjoint workload's mesh,
+        # a short plain run, a short taped run and its reverse, wall-timed
+        from swe_fvm_gb300 import scenarios
         from swe_fvm_gb300.adjoint import Rollout
 
-        ro = Rollout(mesh, prim)
-        gauges = np.arange(0, C, max(1, C // 64))
-        tr = ro.forward(1, args.steps, 10, gauges, 5)
-        ro.backward(np.ones_like(tr))
+        am, ap = scenarios.hump_instance(2024, ADJ_CELLS)
+        am = am.contiguous()
+        gauges = np.random.default_rng(11).choice(am.num_cells, 64, replace=False)
+        ps = SpaceDisc(Fluxes.HLLC(Wavespeeds.Einfeldt), am, ap)
+        ps.set_stream(stream.cuda_stream)
+        ps.run_cfl(1, 2)
+        ps.synchronize()
+        t0 = time.perf_counter()
+        ps.run_cfl(1, args.steps)
+        ps.synchronize()
+        t_plain = time.perf_counter() - t0
+        del ps
+        ro = Rollout(am, ap)
         torch.cuda.synchronize()
-        print(json.dumps({"adjoint_profile": True, "cells": C, "steps": args.steps}))
+        t0 = time.perf_counter()
+        tr = ro.forward(1, args.steps, 50, gauges, 10)
+        t_fwd = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        ro.backward(np.ones_like(tr))
+        t_bwd = time.perf_counter() - t0
+        print(json.dumps({"adjoint_profile": True, "cells": am.num_cells, "steps": args.steps,
+                          "plain_s": t_plain, "taped_forward_s": t_fwd, "backward_s": t_bwd,
+                          "ratio": (t_fwd + t_bwd) / t_plain}))
         return
     if args.profile:
         # profiling driver: warm-up, then exactly K graph-replayed steps

@@ -87,9 +87,12 @@ __global__ void k_seed_gauges(double* lamw, const int* g, int n, const double* g
 }
 
 // ---------------------------------------------------------------- R1: update
+// nst: the stage's conservative state before ConsAssigner ([3][C], kept by the
+// segment recompute), or null to recompute it from the stage's fluxes.
 __global__ void __launch_bounds__(256) k_adj_update(DevMesh m, DevWork wk, AdjWork aw, const double* Wp,
                                                     const double* Up, const double* Vp, const double* W0,
-                                                    const double* U0, const double* V0, Stage st, int batched) {
+                                                    const double* U0, const double* V0, const double* nst, Stage st,
+                                                    int batched) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= m.C) return;
   const int C = m.C;
@@ -98,46 +101,57 @@ __global__ void __launch_bounds__(256) k_adj_update(DevMesh m, DevWork wk, AdjWo
   const unsigned own = m.cown[i];
   const double dti = wk.drain[i];
   const double b = m.bc[i];
-  // ---- forward recompute of the RHS accumulation and the combination
-  double r0 = 0., r1 = 0., r2 = 0.;
+  // ---- draining-limited step of each local edge (as the forward selected it)
   double dtk_[3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
     const int slot = k * C + i;
-    const int e = m.cedge[slot];
-    const double sgn = ((own >> k) & 1u) ? 1. : -1.;
-    const double F0 = wk.f0[e], F1 = wk.f1[e], F2 = wk.f2[e];
+    const double F0 = wk.f0[m.cedge[slot]];
     const int nb = m.cnbr[slot];
     const double dtik = nb < 0 ? kInfA : wk.drain[nb];
-    const double dtk = dgt0(sgn * F0) ? smin(dt, dti) : smin(dt, dtik);
-    dtk_[k] = dtk;
-    const double c_ek = m.cek[slot];
-    const double h_ek = wk.ew[slot] - m.ze[slot];
-    const double s = dtk * sgn * c_ek;
-    r0 -= s * F0;
-    r1 -= s * F1;
-    r2 -= s * F2;
-    const double q = dt * (1. / 3.);
-    r1 -= q * wk.sx[slot] * h_ek;
-    r2 -= q * wk.sy[slot] * h_ek;
-    const double p = 0.5 * h_ek * h_ek;
-    r1 += dtk * (m.cnx[slot] * c_ek * p);
-    r2 += dtk * (m.cny[slot] * c_ek * p);
+    dtk_[k] = dgt0(((own >> k) & 1u) ? F0 : -F0) ? smin(dt, dti) : smin(dt, dtik);
   }
   const double h0 = W0[i] - b;
-  const double c00 = h0, c01 = h0 * U0[i], c02 = h0 * V0[i];
-  double n0, n1, n2, hp = 0., c11 = 0., c12 = 0.;
-  if (st.first) {
-    n0 = c00 + r0;
-    n1 = c01 + r1;
-    n2 = c02 + r2;
+  const double hp = st.first ? 0. : Wp[i] - b;
+  double n0, n1, n2;
+  if (nst) {
+    n0 = nst[i];
+    n1 = nst[C + i];
+    n2 = nst[2 * C + i];
   } else {
-    hp = Wp[i] - b;
-    c11 = hp * Up[i];
-    c12 = hp * Vp[i];
-    n0 = st.a * c00 + st.b * hp + r0;
-    n1 = st.a * c01 + st.b * c11 + r1;
-    n2 = st.a * c02 + st.b * c12 + r2;
+    // forward recompute of the RHS accumulation and the combination
+    double r0 = 0., r1 = 0., r2 = 0.;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const int slot = k * C + i;
+      const int e = m.cedge[slot];
+      const double sgn = ((own >> k) & 1u) ? 1. : -1.;
+      const double F0 = wk.f0[e], F1 = wk.f1[e], F2 = wk.f2[e];
+      const double dtk = dtk_[k];
+      const double c_ek = m.cek[slot];
+      const double h_ek = wk.ew[slot] - m.ze[slot];
+      const double s = dtk * sgn * c_ek;
+      r0 -= s * F0;
+      r1 -= s * F1;
+      r2 -= s * F2;
+      const double q = dt * (1. / 3.);
+      r1 -= q * wk.sx[slot] * h_ek;
+      r2 -= q * wk.sy[slot] * h_ek;
+      const double p = 0.5 * h_ek * h_ek;
+      r1 += dtk * (m.cnx[slot] * c_ek * p);
+      r2 += dtk * (m.cny[slot] * c_ek * p);
+    }
+    const double c00 = h0, c01 = h0 * U0[i], c02 = h0 * V0[i];
+    if (st.first) {
+      n0 = c00 + r0;
+      n1 = c01 + r1;
+      n2 = c02 + r2;
+    } else {
+      const double c11 = hp * Up[i], c12 = hp * Vp[i];
+      n0 = st.a * c00 + st.b * hp + r0;
+      n1 = st.a * c01 + st.b * c11 + r1;
+      n2 = st.a * c02 + st.b * c12 + r2;
+    }
   }
   // ---- reverse of ConsAssigner (src/Assigners.cpp:28-44)
   const double lw = aw.lam[i], lu = aw.lam[C + i], lv = aw.lam[2 * C + i];
@@ -147,16 +161,17 @@ __global__ void __launch_bounds__(256) k_adj_update(DevMesh m, DevWork wk, AdjWo
   } else {
     double ih, dih;
     if (dltc(n0, kEta1)) {
-      const double h4 = n0 * n0 * n0 * n0 + kEta4;
+      const double n2_ = n0 * n0;
+      const double h4 = fma(n2_, n2_, kEta4);
       const double sq = SWE_SQRT(h4);
-      ih = SWE_DIV(kSqrt2 * n0, sq);
-      dih = SWE_DIV(kSqrt2 * (kEta4 - n0 * n0 * n0 * n0), h4 * sq);
+      ih = kSqrt2 * n0 * SWE_DIV(1., sq);
+      dih = kSqrt2 * fma(-n2_, n2_, kEta4) * SWE_DIV(1., h4 * sq);
     } else {
       ih = SWE_DIV(1., n0);
       dih = -ih * ih;
     }
     lbc += lw;
-    ln0 = lw + (lu * n1 + lv * n2) * dih;
+    ln0 = fma(fma(lu, n1, lv * n2), dih, lw);
     ln1 = lu * ih;
     ln2 = lv * ih;
   }
@@ -164,45 +179,45 @@ __global__ void __launch_bounds__(256) k_adj_update(DevMesh m, DevWork wk, AdjWo
   const double a0c = st.first ? 1. : st.a;
   const double lc00 = a0c * ln0, lc01 = a0c * ln1, lc02 = a0c * ln2;
   {
-    const double lh0 = lc00 + lc01 * U0[i] + lc02 * V0[i];
+    const double lh0 = fma(lc01, U0[i], fma(lc02, V0[i], lc00));
     aw.lam0[i] += lh0;
-    aw.lam0[C + i] += lc01 * h0;
-    aw.lam0[2 * C + i] += lc02 * h0;
+    aw.lam0[C + i] = fma(lc01, h0, aw.lam0[C + i]);
+    aw.lam0[2 * C + i] = fma(lc02, h0, aw.lam0[2 * C + i]);
     lbc -= lh0;
   }
   if (!st.first) {
     const double lc10 = st.b * ln0, lc11 = st.b * ln1, lc12 = st.b * ln2;
-    const double lhp = lc10 + lc11 * Up[i] + lc12 * Vp[i];
+    const double lhp = fma(lc11, Up[i], fma(lc12, Vp[i], lc10));
     aw.lamp[i] += lhp;
-    aw.lamp[C + i] += lc11 * hp;
-    aw.lamp[2 * C + i] += lc12 * hp;
+    aw.lamp[C + i] = fma(lc11, hp, aw.lamp[C + i]);
+    aw.lamp[2 * C + i] = fma(lc12, hp, aw.lamp[2 * C + i]);
     lbc -= lhp;
   }
   // ---- reverse of the RHS (src/TimeDisc.cpp:21-36), per local edge
   const double q = dt * (1. / 3.);
+  const double ln1q = ln1 * q, ln2q = ln2 * q;
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
     const int slot = k * C + i;
     const int e = m.cedge[slot];
-    const double sgn = ((own >> k) & 1u) ? 1. : -1.;
+    const bool out = (own >> k) & 1u;
     const double F0 = wk.f0[e], F1 = wk.f1[e], F2 = wk.f2[e];
     const double c_ek = m.cek[slot];
     const double h_ek = wk.ew[slot] - m.ze[slot];
     const double p = 0.5 * h_ek * h_ek;
     const double dtk = dtk_[k];
-    const double s = dtk * sgn * c_ek;
+    const double sc = out ? c_ek : -c_ek;  // sgn c_ek
+    const double s = dtk * sc;
     const double nxc = m.cnx[slot] * c_ek, nyc = m.cny[slot] * c_ek;
-    double ldtk = ln1 * (nxc * p) + ln2 * (nyc * p);
-    const double lp = dtk * (ln1 * nxc + ln2 * nyc);
-    double lh = lp * h_ek;
-    aw.lsx[slot] = -ln1 * q * h_ek;
-    aw.lsy[slot] = -ln2 * q * h_ek;
-    lh -= ln1 * q * wk.sx[slot] + ln2 * q * wk.sy[slot];
-    const double ls = -(ln0 * F0 + ln1 * F1 + ln2 * F2);
+    const double lpn = fma(ln1, nxc, ln2 * nyc);
+    const double ls = -fma(ln0, F0, fma(ln1, F1, ln2 * F2));
+    const double ldtk = fma(ls, sc, lpn * p);
+    const double lh = fma(dtk * lpn, h_ek, -fma(ln1q, wk.sx[slot], ln2q * wk.sy[slot]));
+    aw.lsx[slot] = -ln1q * h_ek;
+    aw.lsy[slot] = -ln2q * h_ek;
     aw.lF0[slot] = -ln0 * s;
     aw.lF1[slot] = -ln1 * s;
     aw.lF2[slot] = -ln2 * s;
-    ldtk += ls * sgn * c_ek;
     aw.lew[slot] = lh;
     aw.leu[slot] = 0.;
     aw.lev[slot] = 0.;
@@ -210,7 +225,7 @@ __global__ void __launch_bounds__(256) k_adj_update(DevMesh m, DevWork wk, AdjWo
     // route of the draining time step actually selected by min(dt, .)
     const int nb = m.cnbr[slot];
     int route = 0;
-    if (dgt0(sgn * F0)) {
+    if (dgt0(out ? F0 : -F0)) {
       if (dlt(dti, dt)) route = 1;
     } else if (nb >= 0) {
       if (dlt(wk.drain[nb], dt)) route = 2;
@@ -311,7 +326,9 @@ struct P1 {
   bool kept;
   double w0;
 };
-__device__ P1 pass1(const DevMesh& m, const double* W, int c) {
+// pwrec: the PartWet1 levels the forward pass 1 stored for its partially-wet
+// cells (read instead of repeating the cubic solve).
+__device__ P1 pass1(const DevMesh& m, const double* W, int c, const double* pwrec) {
   P1 r{0, 0, false, 0.};
   const int C = m.C;
   const double w = W[c];
@@ -319,11 +336,7 @@ __device__ P1 pass1(const DevMesh& m, const double* W, int c) {
   if (!is_wet(h)) return r;
   if (!dlt(m.fwthr[c], w)) {
     r.type = 1;
-    const double* p = m.pw1 + (size_t)c * kPw1Stride;
-    const double b13 = p[0], b23 = p[1], bdel = p[3];
-    if (dle(b13, w)) r.w0 = w;
-    else if (dle(w, bdel)) r.w0 = b23 + cbrt_rn(3. * h * p[6] * p[7]);
-    else r.w0 = bisection(p[6] * (3. * h * p[8] - p[9]) - p[10], p[5], p[4], p[2], b13);
+    r.w0 = pwrec[c];
     return r;
   }
   r.type = 2;
@@ -355,10 +368,10 @@ __device__ P1 pass1(const DevMesh& m, const double* W, int c) {
 
 // Pass-1 value of cell c at its local node kn (AtPoint(P).w), and where its
 // derivative goes: dstate = d value / d W[c]; static part to node z.
-__device__ double pass1_node_value(const DevMesh& m, const double* W, int c, int kn) {
+__device__ double pass1_node_value(const DevMesh& m, const double* W, int c, int kn, const double* pwrec) {
   const int C = m.C;
   const double z = m.zn[kn * C + c];
-  const P1 p = pass1(m, W, c);
+  const P1 p = pass1(m, W, c, pwrec);
   if (p.type == 0) return m.dry[(size_t)c * kDryStride + kn];
   double off = 0.;
   if (p.type == 2 && p.kept) off = m.combo[((size_t)c * 8 + p.mask) * kComboStride + 8 + kn];
@@ -387,7 +400,7 @@ __device__ __forceinline__ void lam_cell_z(const DevMesh& m, AdjWork& aw, int c,
 // PartWet1 level and its derivatives with respect to (w, z0, z1, z2) of the
 // cell (src/MUSCLObject.cpp:86-112), recomputed from the node bathymetry.
 template <class T>
-__device__ T partwet1_t(const T& w, const T& z0, const T& z1, const T& z2) {
+__device__ T partwet1_t(const T& w, const T& z0, const T& z1, const T& z2, double root) {
   const double k3 = 1. / 3.;
   T bc = z0 * k3 + z1 * k3 + z2 * k3;
   T h = w - bc;
@@ -403,6 +416,8 @@ __device__ T partwet1_t(const T& w, const T& z0, const T& z1, const T& z2) {
   T a = -3. * b13;
   T bb = 3. * (b12 * b13 + b13 * b23 - b12 * b23);
   T cc = (b13 - b23) * (3. * h * (b13 - b12) - b12 * (b12 + b23)) - b23 * b23 * b13;
+  // root: the level the forward pass found (the same cubic's root)
+  if (dle(val(b12), root) && dle(root, val(b13))) return bisection_root_t(cc, bb, a, val(b12), val(b13), root);
   return bisection_t(cc, bb, a, val(b12), val(b13));
 }
 
@@ -545,10 +560,11 @@ __device__ void combo_points_to_nodes(const DevMesh& m, AdjWork& aw, int c, int 
   }
 }
 
-__global__ void __launch_bounds__(256) k_adj_recon(DevMesh m, DevWork wk, AdjWork aw, const double* W,
-                                                   const double* U, const double* V, int batched) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= m.C) return;
+// Reverse of the reconstruction of cell i.  PASS 1: dry and fully-wet cells;
+// PASS 2: partially-wet cells only.
+template <int PASS>
+__device__ void adj_recon_cell(const DevMesh& m, const DevWork& wk, AdjWork aw, const double* W, const double* U,
+                               const double* V, int i, int batched) {
   const int C = m.C;
   const int inst = batched ? m.cinst[i] : 0;
   const double cor = m.inst_cor[inst];
@@ -564,14 +580,17 @@ __global__ void __launch_bounds__(256) k_adj_recon(DevMesh m, DevWork wk, AdjWor
       lbc -= lh;
     }
   }
-  const P1 p = pass1(m, W, i);
+  const P1 p = pass1(m, W, i, wk.pwrec);
+  if ((PASS == 1 && p.type == 1) || (PASS == 2 && p.type != 1)) return;
   // forward description of the final interface values: level w0 + off_k, velocity, slope
   double w0 = w, gx = 0., gy = 0., off[3] = {0., 0., 0.};
   double u0 = u, v0 = v;
   bool pw2_plane = false;
   double w23 = 0.;
   int lo_node = -1;
-  if (p.type == 0) {
+  typedef Dual<5> D5;  // PartWet2 over (w, w23, z_lo, z_mid, z_hi)
+  D5 w0D, gxD, gyD;
+  if (PASS == 1 && p.type == 0) {
     const double* dr = m.dry + (size_t)i * kDryStride;
     // interface values (dew_k, 0, 0) and slope (sx, sy): all bathymetry
     for (int k = 0; k < 3; ++k) {
@@ -601,7 +620,7 @@ __global__ void __launch_bounds__(256) k_adj_recon(DevMesh m, DevWork wk, AdjWor
     lam_cell_z(m, aw, i, lbc);
     return;
   }
-  if (p.type == 2) {
+  if (PASS == 1) {
     w0 = w;
     if (p.kept) {
       const double* rec = m.combo + ((size_t)i * 8 + p.mask) * kComboStride;
@@ -610,17 +629,23 @@ __global__ void __launch_bounds__(256) k_adj_recon(DevMesh m, DevWork wk, AdjWor
       for (int k = 0; k < 3; ++k) off[k] = rec[5 + k];
     }
   } else {
-    // partially wet: PartWet2 with the pass-1 maxima, else PartWet1
+    // partially wet: PartWet2 with the pass-1 maxima, else PartWet1; the dual
+    // evaluation gives the forward values bit for bit and their derivatives
     const Pw2Rec& r = m.pw2[i];
     lo_node = r.lo;
     w23 = order_val(wk.maxwp[r.lo]);
-    const double bcv = m.bc[i];
-    double w0d, gxd, gyd;
-    pw2_plane = partwet2_t(r, w, w23, r.p[0][2], r.p[1][2], r.p[2][2], bcv, &w0d, &gxd, &gyd);
+    D5 zc[3];
+    for (int k = 0; k < 3; ++k) zc[k] = D5(m.zn[k * C + i]);
+    const D5 zl = D5::var(r.p[0][2], 2), zm = D5::var(r.p[1][2], 3), zh = D5::var(r.p[2][2], 4);
+    for (int s = 0; s < 3; ++s) zc[r.sk[s]] = (s == 0) ? zl : (s == 1 ? zm : zh);
+    const double k3 = 1. / 3.;
+    D5 bcd = zc[0] * k3 + zc[1] * k3 + zc[2] * k3;
+    bcd.v = m.bc[i];  // the forward's centroid bathymetry
+    pw2_plane = partwet2_t(r, D5::var(w, 0), D5::var(w23, 1), zl, zm, zh, bcd, &w0D, &gxD, &gyD);
     if (pw2_plane) {
-      w0 = w0d;
-      gx = gxd;
-      gy = gyd;
+      w0 = w0D.v;
+      gx = gxD.v;
+      gy = gyD.v;
       for (int k = 0; k < 3; ++k) off[k] = gx * r.dedge[k][0] + gy * r.dedge[k][1];
     } else {
       w0 = p.w0;
@@ -641,7 +666,7 @@ __global__ void __launch_bounds__(256) k_adj_recon(DevMesh m, DevWork wk, AdjWor
     lgy += lgyk;
     lam_edge_z(m, aw, i, k, lze + aw.lze[slot]);
   }
-  if (p.type == 2) {
+  if (PASS == 1) {
     lw_i += lw0;
     if (p.kept) {
       // the combination plane through neighbour centroids / edge centres
@@ -661,17 +686,10 @@ __global__ void __launch_bounds__(256) k_adj_recon(DevMesh m, DevWork wk, AdjWor
     const Pw2Rec& r = m.pw2[i];
     int sorted_local[3] = {r.sk[0], r.sk[1], r.sk[2]};
     if (pw2_plane) {
-      typedef Dual<5> D;
-      D wd = D::var(w, 0), w23d = D::var(w23, 1);
-      D zl = D::var(r.p[0][2], 2), zm = D::var(r.p[1][2], 3), zh = D::var(r.p[2][2], 4);
       const double k3 = 1. / 3.;
-      // bc as a function of the three node z (in cell order)
-      D zc[3];
-      for (int k = 0; k < 3; ++k) zc[k] = D(m.zn[k * C + i]);
-      for (int s = 0; s < 3; ++s) zc[sorted_local[s]] = (s == 0) ? zl : (s == 1 ? zm : zh);
-      D bcd = zc[0] * k3 + zc[1] * k3 + zc[2] * k3;
-      D w0d, gxd, gyd;
-      partwet2_t(r, wd, w23d, zl, zm, zh, bcd, &w0d, &gxd, &gyd);
+      const D5& w0d = w0D;
+      const D5& gxd = gxD;
+      const D5& gyd = gyD;
       double lg0 = lgx, lg1 = lgy;
       for (int k = 0; k < 3; ++k) {
         lg0 += loff[k] * r.dedge[k][0];
@@ -689,7 +707,7 @@ __global__ void __launch_bounds__(256) k_adj_recon(DevMesh m, DevWork wk, AdjWor
         int best = -1, bestk = 0;
         for (int q = aw.node_ptr[nd]; q < aw.node_ptr[nd + 1]; ++q) {
           const int c = aw.node_cells[q] >> 2, kn = aw.node_cells[q] & 3;
-          const double val_c = pass1_node_value(m, W, c, kn);
+          const double val_c = pass1_node_value(m, W, c, kn, wk.pwrec);
           if (val_c == w23) {
             best = c;
             bestk = kn;
@@ -699,7 +717,7 @@ __global__ void __launch_bounds__(256) k_adj_recon(DevMesh m, DevWork wk, AdjWor
         if (best < 0) {
           atomicAdd(aw.lz + nd, g[1]);  // the maximum is the node bathymetry itself
         } else {
-          const P1 pc = pass1(m, W, best);
+          const P1 pc = pass1(m, W, best, wk.pwrec);
           const double zc_ = m.zn[bestk * C + best];
           if (pc.type == 0) {
             // dry plane value at the node: a function of bathymetry only
@@ -735,7 +753,8 @@ __global__ void __launch_bounds__(256) k_adj_recon(DevMesh m, DevWork wk, AdjWor
             } else {
               typedef Dual<4> F4;
               F4 wb = F4::var(W[best], 0);
-              F4 y = partwet1_t(wb, F4::var(m.zn[best], 1), F4::var(m.zn[C + best], 2), F4::var(m.zn[2 * C + best], 3));
+              F4 y = partwet1_t(wb, F4::var(m.zn[best], 1), F4::var(m.zn[C + best], 2), F4::var(m.zn[2 * C + best], 3),
+                                pc.w0);
               atomicAdd(aw.lscatter + best, g[1] * y.d[0]);
               for (int q = 0; q < 3; ++q)
                 if (y.d[1 + q] != 0.) atomicAdd(aw.lz + cnode(m, best, q), g[1] * y.d[1 + q]);
@@ -746,7 +765,7 @@ __global__ void __launch_bounds__(256) k_adj_recon(DevMesh m, DevWork wk, AdjWor
     } else {
       // PartWet1 level: dual over (w, z0, z1, z2)
       typedef Dual<4> D;
-      D y = partwet1_t(D::var(w, 0), D::var(m.zn[i], 1), D::var(m.zn[C + i], 2), D::var(m.zn[2 * C + i], 3));
+      D y = partwet1_t(D::var(w, 0), D::var(m.zn[i], 1), D::var(m.zn[C + i], 2), D::var(m.zn[2 * C + i], 3), p.w0);
       lw_i += lw0 * y.d[0];
       for (int q = 0; q < 3; ++q)
         if (y.d[1 + q] != 0.) atomicAdd(aw.lz + cnode(m, i, q), lw0 * y.d[1 + q]);
@@ -756,6 +775,21 @@ __global__ void __launch_bounds__(256) k_adj_recon(DevMesh m, DevWork wk, AdjWor
   aw.lamp[C + i] += lu_i;
   aw.lamp[2 * C + i] += lv_i;
   lam_cell_z(m, aw, i, lbc);
+}
+
+__global__ void __launch_bounds__(256) k_adj_recon(DevMesh m, DevWork wk, AdjWork aw, const double* W,
+                                                   const double* U, const double* V, int batched) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < m.C) adj_recon_cell<1>(m, wk, aw, W, U, V, i, batched);
+}
+
+// partially-wet cells of the stage (the list pass 1 of the forward wrote)
+// (one warp per block: the few listed cells spread over many SMs)
+__global__ void __launch_bounds__(32) k_adj_recon_pw(DevMesh m, DevWork wk, AdjWork aw, const double* W,
+                                                     const double* U, const double* V, int batched) {
+  const int n = min(*wk.pwcount, m.C);
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x)
+    adj_recon_cell<2>(m, wk, aw, W, U, V, wk.pwlist[q], batched);
 }
 
 }  // namespace
@@ -773,6 +807,8 @@ struct AdjointState {
   double* d_dt = nullptr;            // [n_steps] recorded dt
   double* d_traces = nullptr;        // [n_obs x n_gauges]
   bool taped = false;
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   template <class T>
   T* alloc(size_t n) {
     void* p = nullptr;
@@ -793,6 +829,9 @@ struct AdjointState {
   ~AdjointState() {
     free_tape();
     for (void* p : allocs) cudaFree(p);
+    if (side) cudaStreamDestroy(side);
+    if (ev_fork) cudaEventDestroy(ev_fork);
+    if (ev_join) cudaEventDestroy(ev_join);
   }
 };
 
@@ -858,6 +897,12 @@ std::string Engine::adjoint_init() {
   w.node_cells = d_cells;
   w.edge_nodes = d_en;
   cudaMemset(w.lscatter, 0, C * sizeof(double));
+  if (cudaStreamCreateWithFlags(&a->side, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&a->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&a->ev_join, cudaEventDisableTiming) != cudaSuccess) {
+    delete a;
+    return "adjoint stream set-up failed";
+  }
   adj_ = a;
   return "";
 }
@@ -944,6 +989,51 @@ std::string Engine::adjoint_backward(const double* trace_grads_host, double* gra
         if (q) cudaFree(q);
       return "segment store allocation failed";
     }
+  const int b = 256, gc = (int)((C + b - 1) / b);
+  // per-stage forward intermediates of one segment (interface slots, fluxes,
+  // draining dt, node maxima, part-wet list) when device memory allows
+  const int64_t E = mesh_.E;
+  const size_t per_stage = ((15 * C + 3 * E + 5 * C) * sizeof(double) + N * sizeof(unsigned long long) +
+                            (C + 1) * sizeof(int) + 255) / 256 * 256;
+  size_t free_b = 0, total_b = 0;
+  cudaMemGetInfo(&free_b, &total_b);
+  const bool keep = (double)per_stage * (double)(K * ns) < 0.6 * (double)free_b;
+  std::vector<DevWork> kept;
+  std::vector<double*> kept_n;  // state before ConsAssigner of each stage
+  char* kept_pool = nullptr;
+  if (keep) {
+    if (cudaMalloc(&kept_pool, per_stage * (size_t)(K * ns)) != cudaSuccess) {
+      cudaFree(d_tg);
+      for (auto& q : store) cudaFree(q);
+      return "intermediate store allocation failed";
+    }
+    kept.resize((size_t)(K * ns));
+    kept_n.resize((size_t)(K * ns));
+    for (int64_t q = 0; q < K * ns; ++q) {
+      char* p = kept_pool + per_stage * (size_t)q;
+      DevWork wq = work_;
+      auto take = [&](size_t bytes) {
+        char* r = p;
+        p += bytes;
+        return r;
+      };
+      wq.ew = (double*)take(3 * C * sizeof(double));
+      wq.eu = (double*)take(3 * C * sizeof(double));
+      wq.ev = (double*)take(3 * C * sizeof(double));
+      wq.sx = (double*)take(3 * C * sizeof(double));
+      wq.sy = (double*)take(3 * C * sizeof(double));
+      wq.f0 = (double*)take(E * sizeof(double));
+      wq.f1 = (double*)take(E * sizeof(double));
+      wq.f2 = (double*)take(E * sizeof(double));
+      wq.drain = (double*)take(C * sizeof(double));
+      wq.pwrec = (double*)take(C * sizeof(double));
+      wq.maxwp = (unsigned long long*)take(N * sizeof(unsigned long long));
+      wq.pwlist = (int*)take(C * sizeof(int));
+      kept_n[q] = (double*)take(3 * C * sizeof(double));
+      wq.pwcount = (int*)take(sizeof(int));
+      kept[q] = wq;
+    }
+  }
   double* lam_cur = w.lam;
   cudaMemsetAsync(w.lam, 0, 3 * C * sizeof(double), stream_);
   cudaMemsetAsync(w.lz, 0, N * sizeof(double), stream_);
@@ -954,12 +1044,12 @@ std::string Engine::adjoint_backward(const double* trace_grads_host, double* gra
   double* lam_step = nullptr;  // adjoint of the current step's end state
   cudaMalloc(&lam_step, 3 * C * sizeof(double));
   cudaMemsetAsync(lam_step, 0, 3 * C * sizeof(double), stream_);
-  const int b = 256, gc = (int)((C + b - 1) / b);
   std::string err;
   const int64_t nseg = (a.n_steps + K - 1) / K;
   for (int64_t seg = nseg - 1; seg >= 0 && err.empty(); --seg) {
     const int64_t s0 = seg * K, s1 = std::min(a.n_steps, s0 + K);
-    // recompute the segment stage by stage with the recorded dt
+    // recompute the segment stage by stage with the recorded dt, keeping every
+    // stage's forward intermediates when they fit
     for (int q = 0; q < 3; ++q)
       cudaMemcpyAsync(store[0] + q * C, a.checkpoints[seg] + q * C, C * sizeof(double), cudaMemcpyDeviceToDevice,
                       stream_);
@@ -973,8 +1063,22 @@ std::string Engine::adjoint_backward(const double* trace_grads_host, double* gra
         double* outp = store[base + s + 1];
         const double* in[3] = {inp, inp + C, inp + 2 * C};
         double* out[3] = {outp, outp + C, outp + 2 * C};
-        cudaError_t e = reset_pass();
-        if (e == cudaSuccess) e = launch_stage(sc.s[s], in, u0, out, s == 0, s == 0 ? 2 : 0);
+        cudaError_t e;
+        if (keep) {
+          const DevWork saved = work_;
+          work_ = kept[base + s];
+          e = reset_pass();
+          if (e == cudaSuccess) e = interface_values(in[0], in[1], in[2], s == 0 ? 2 : 0);
+          if (e == cudaSuccess) e = fluxes(in[0]);
+          if (e == cudaSuccess) {
+            k_drain_keep<<<gc, b, 0, stream_>>>(mesh_, work_, in[0]);
+            e = update_only(sc.s[s], in, u0, out, kept_n[base + s]);
+          }
+          work_ = saved;
+        } else {
+          e = reset_pass();
+          if (e == cudaSuccess) e = launch_stage(sc.s[s], in, u0, out, s == 0, s == 0 ? 2 : 0);
+        }
         if (e != cudaSuccess) {
           err = std::string("segment recompute: ") + cudaGetErrorString(e);
           break;
@@ -1000,7 +1104,8 @@ std::string Engine::adjoint_backward(const double* trace_grads_host, double* gra
         double* inp = store[base + s];
         const double* in[3] = {inp, inp + C, inp + 2 * C};
         cudaMemsetAsync(w.lamp, 0, 3 * C * sizeof(double), stream_);
-        cudaError_t e = adjoint_stage_reverse(sc.s[s], in, u0, w);
+        cudaError_t e = keep ? adjoint_stage_reverse_stored(sc.s[s], in, u0, w, kept[base + s], kept_n[base + s])
+                             : adjoint_stage_reverse(sc.s[s], in, u0, w);
         if (e != cudaSuccess) {
           err = std::string("stage reverse: ") + cudaGetErrorString(e);
           break;
@@ -1023,6 +1128,7 @@ std::string Engine::adjoint_backward(const double* trace_grads_host, double* gra
     if (e != cudaSuccess) err = std::string("adjoint: ") + cudaGetErrorString(e);
   }
   cudaMemcpy(work_.tsum, &tsum_saved, sizeof(double), cudaMemcpyHostToDevice);
+  if (kept_pool) cudaFree(kept_pool);
   for (auto& p : store) cudaFree(p);
   cudaFree(d_tg);
   cudaFree(lam_step);
@@ -1031,25 +1137,40 @@ std::string Engine::adjoint_backward(const double* trace_grads_host, double* gra
 
 cudaError_t Engine::adjoint_stage_reverse(const Stage& st, const double* const* in, const double* const* u0,
                                           AdjWork& aw) {
-  const int b = 256;
-  const int gc = (mesh_.C + b - 1) / b, ge = (mesh_.E + b - 1) / b;
-  // recompute the stage's forward intermediates from its input
+  // recompute the stage's forward intermediates from its input into work_
   cudaError_t e = reset_pass();
   if (e == cudaSuccess) e = interface_values(in[0], in[1], in[2], 0);
   if (e == cudaSuccess) e = fluxes(in[0]);
   if (e != cudaSuccess) return e;
-  k_drain_keep<<<gc, b, 0, stream_>>>(mesh_, work_, in[0]);
-  k_adj_update<<<gc, b, 0, stream_>>>(mesh_, work_, aw, in[0], in[1], in[2], u0[0], u0[1], u0[2], st, batched_);
-  k_adj_drain<<<gc, b, 0, stream_>>>(mesh_, work_, aw, in[0]);
+  const int b = 256;
+  k_drain_keep<<<(mesh_.C + b - 1) / b, b, 0, stream_>>>(mesh_, work_, in[0]);
+  ++launches_;
+  return adjoint_stage_reverse_stored(st, in, u0, aw, work_, nullptr);
+}
+
+cudaError_t Engine::adjoint_stage_reverse_stored(const Stage& st, const double* const* in, const double* const* u0,
+                                                 AdjWork& aw, const DevWork& wk, const double* nst) {
+  const int b = 256;
+  const int gc = (mesh_.C + b - 1) / b, ge = (mesh_.E + b - 1) / b;
+  k_adj_update<<<gc, b, 0, stream_>>>(mesh_, wk, aw, in[0], in[1], in[2], u0[0], u0[1], u0[2], nst, st, batched_);
+  k_adj_drain<<<gc, b, 0, stream_>>>(mesh_, wk, aw, in[0]);
   switch (flux_ * 3 + ws_) {
-    case 0: k_adj_flux<0, 0><<<ge, b, 0, stream_>>>(mesh_, work_, aw, in[0]); break;
-    case 1: k_adj_flux<0, 1><<<ge, b, 0, stream_>>>(mesh_, work_, aw, in[0]); break;
-    case 2: k_adj_flux<0, 2><<<ge, b, 0, stream_>>>(mesh_, work_, aw, in[0]); break;
-    case 3: k_adj_flux<1, 0><<<ge, b, 0, stream_>>>(mesh_, work_, aw, in[0]); break;
-    case 4: k_adj_flux<1, 1><<<ge, b, 0, stream_>>>(mesh_, work_, aw, in[0]); break;
-    default: k_adj_flux<1, 2><<<ge, b, 0, stream_>>>(mesh_, work_, aw, in[0]); break;
+    case 0: k_adj_flux<0, 0><<<ge, b, 0, stream_>>>(mesh_, wk, aw, in[0]); break;
+    case 1: k_adj_flux<0, 1><<<ge, b, 0, stream_>>>(mesh_, wk, aw, in[0]); break;
+    case 2: k_adj_flux<0, 2><<<ge, b, 0, stream_>>>(mesh_, wk, aw, in[0]); break;
+    case 3: k_adj_flux<1, 0><<<ge, b, 0, stream_>>>(mesh_, wk, aw, in[0]); break;
+    case 4: k_adj_flux<1, 1><<<ge, b, 0, stream_>>>(mesh_, wk, aw, in[0]); break;
+    default: k_adj_flux<1, 2><<<ge, b, 0, stream_>>>(mesh_, wk, aw, in[0]); break;
   }
-  k_adj_recon<<<gc, b, 0, stream_>>>(mesh_, work_, aw, in[0], in[1], in[2], batched_);
+  // partially-wet cells on a side stream, overlapping the rest of the reconstruction reverse
+  AdjointState& a = *adj_;
+  cudaEventRecord(a.ev_fork, stream_);
+  cudaStreamWaitEvent(a.side, a.ev_fork, 0);
+  const int gpw = std::max(1, std::min((mesh_.C + 31) / 32, 152 * 16));
+  k_adj_recon_pw<<<gpw, 32, 0, a.side>>>(mesh_, wk, aw, in[0], in[1], in[2], batched_);
+  cudaEventRecord(a.ev_join, a.side);
+  k_adj_recon<<<gc, b, 0, stream_>>>(mesh_, wk, aw, in[0], in[1], in[2], batched_);
+  cudaStreamWaitEvent(stream_, a.ev_join, 0);
   launches_ += 5;
   return cudaGetLastError();
 }

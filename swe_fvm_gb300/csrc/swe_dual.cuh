@@ -6,7 +6,8 @@
 // swe_physics.cuh, so the value part of a Dual evaluation is bit-identical to
 // the forward step and every branch (dry clamps, limiter, min/max selections,
 // wet/dry thresholds) is taken exactly as in the forward pass; derivatives are
-// those of the branch taken.  Derivatives of sqrt at 0 are taken as 0: a zero
+// those of the branch taken; derivative parts use explicit fused
+// multiply-adds (values never do).  Derivatives of sqrt at 0 are taken as 0: a zero
 // depth only reaches sqrt from a dry-clamped interface value, which is
 // locally constant.
 #pragma once
@@ -59,14 +60,15 @@ SWE_HD Dual<N> operator-(const Dual<N>& a) {
 template <int N>
 SWE_HD Dual<N> operator*(const Dual<N>& a, const Dual<N>& b) {
   Dual<N> r(a.v * b.v);
-  for (int k = 0; k < N; ++k) r.d[k] = a.d[k] * b.v + a.v * b.d[k];
+  for (int k = 0; k < N; ++k) r.d[k] = fma(a.d[k], b.v, a.v * b.d[k]);
   return r;
 }
 template <int N>
 SWE_HD Dual<N> operator/(const Dual<N>& a, const Dual<N>& b) {
-  const double q = SWE_DIV(a.v, b.v);
+  const double q = SWE_DIV(a.v, b.v);  // the value keeps the exact quotient
   Dual<N> r(q);
-  for (int k = 0; k < N; ++k) r.d[k] = SWE_DIV(a.d[k] - q * b.d[k], b.v);
+  const double ib = SWE_DIV(1., b.v);
+  for (int k = 0; k < N; ++k) r.d[k] = fma(-q, b.d[k], a.d[k]) * ib;
   return r;
 }
 template <int N>
@@ -269,6 +271,19 @@ SWE_HD Dual<N> bisection_t(const Dual<N>& d, const Dual<N>& c, const Dual<N>& b,
 }
 SWE_HD double bisection_t(double d, double c, double b, double xmin, double xmax) {
   return bisection(d, c, b, xmin, xmax);
+}
+// bisection_t when the forward pass already found the root x: the same value
+// and implicit-function derivatives without repeating the bisection.
+template <int N>
+SWE_HD Dual<N> bisection_root_t(const Dual<N>& d, const Dual<N>& c, const Dual<N>& b, double xmin, double xmax,
+                                double x) {
+  Dual<N> r(x);
+  const double f0 = cubic(d.v, c.v, b.v, xmin), f1 = cubic(d.v, c.v, b.v, xmax);
+  if (signbit(f0) == signbit(f1)) return r;
+  const double fp = 3. * x * x + 2. * b.v * x + c.v;
+  if (fp == 0.) return r;
+  for (int k = 0; k < N; ++k) r.d[k] = -SWE_DIV(d.d[k] + c.d[k] * x + b.d[k] * x * x, fp);
+  return r;
 }
 
 // cube root with derivative (1/3) x^(-2/3); 0 at 0

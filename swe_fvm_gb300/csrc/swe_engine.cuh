@@ -159,6 +159,12 @@ class Engine {
   // `in` and whose step started from `u0`, given aw.lam; accumulates aw.lamp,
   // aw.lam0, aw.lz.
   cudaError_t adjoint_stage_reverse(const Stage& st, const double* const* in, const double* const* u0, AdjWork& aw);
+  cudaError_t adjoint_stage_reverse_stored(const Stage& st, const double* const* in, const double* const* u0,
+                                           AdjWork& aw, const DevWork& wk, const double* nst);
+  // the update kernel of one stage alone (the rest of the stage already ran),
+  // also keeping the state before ConsAssigner in nst [3][C]
+  cudaError_t update_only(const Stage& st, const double* const* in, const double* const* u0, double* const* out,
+                          double* nst);
   // Taped forward run for the adjoint: n_steps CFL steps from the current
   // state, checkpoint every ckpt steps, w at the gauge cells every obs steps
   // into traces_host (n_steps / obs rows).  Returns "" or an error message.

@@ -6,34 +6,82 @@
 // interface states and the edge bathymetry, following the branches the forward
 // took.  It matches the forward-mode Jacobian of flux_t (swe_dual.cuh); the
 // self-test swe_selftest_flux_adjoint compares the two.
+//
+// Every value that steers a branch (depths, normal velocities, wave speeds,
+// u*) is recomputed with the forward's own operations, so it is bit-identical
+// to the forward pass.  Quantities that only feed derivatives use explicit
+// fused multiply-adds: the library is compiled without FMA contraction (the
+// forward must round like the reference), and one DFMA costs the FP64 pipe as
+// much as one DMUL.
 #pragma once
 
 #include "swe_physics.cuh"
 
 namespace swe {
 
-// ElemFlux(n, (h, hu, hv)) reverse: adds to lh, lhu, lhv
-SWE_HD void elem_flux_rev(double nx, double ny, double h, double hu, double hv, const double* lf, double* lh,
-                          double* lhu, double* lhv) {
+// Forward wave speeds (src/Fluxes.cpp:5-26) with the intermediates the reverse
+// reads; the same operations as the plugins' speeds().
+struct WsFwd {
+  double cl, cr, S, uRoe, cRoe, a0, a1;
+};
+SWE_HD WsFwd ws_forward(int ws, double ul, double hl, double ur, double hr) {
+  WsFwd f;
+  f.cl = SWE_SQRT(hl);
+  f.cr = SWE_SQRT(hr);
+  f.S = 0.;
+  f.uRoe = 0.;
+  f.cRoe = 0.;
+  if (ws == 0) {
+    const double ap = smax(fabs(ul) + f.cl, fabs(ur) + f.cr);
+    f.a0 = -ap;
+    f.a1 = ap;
+  } else if (ws == 1) {
+    f.a0 = smin(ul - f.cl, ur - f.cr);
+    f.a1 = smax(ul + f.cl, ur + f.cr);
+  } else {
+    f.S = f.cl + f.cr;
+    f.uRoe = SWE_DIV(f.cl * ul + f.cl * ur, f.S);
+    f.cRoe = SWE_SQRT(0.5 * (hl + hr));
+    f.a0 = smin(ul - f.cl, f.uRoe - f.cRoe);
+    f.a1 = smax(ur + f.cr, f.uRoe + f.cRoe);
+  }
+  return f;
+}
+
+// ElemFlux(n, (h, hu, hv)) (include/SpaceDisc.h:4-18) for derivative use only
+SWE_HD void elem_flux_fma(double nx, double ny, double h, double hu, double hv, double ih, double* f) {
+  f[0] = 0.;
+  f[1] = 0.;
+  f[2] = 0.;
+  if (is_wet(h)) {
+    const double hveln = fma(hu, nx, hv * ny);
+    const double q = hveln * ih;
+    const double p = 0.5 * h * h;
+    f[0] = hveln;
+    f[1] = fma(q, hu, p * nx);
+    f[2] = fma(q, hv, p * ny);
+  }
+}
+
+// ElemFlux reverse: adds to lh, lhu, lhv (ih = 1 / h)
+SWE_HD void elem_flux_rev(double nx, double ny, double h, double hu, double hv, double ih, const double* lf,
+                          double* lh, double* lhu, double* lhv) {
   if (!is_wet(h)) return;
-  const double hveln = hu * nx + hv * ny;
-  const double q = SWE_DIV(hveln, h);
-  const double lq = lf[1] * hu + lf[2] * hv;
-  const double lhveln = lf[0] + SWE_DIV(lq, h);
-  *lhu += lf[1] * q + lhveln * nx;
-  *lhv += lf[2] * q + lhveln * ny;
-  *lh += -SWE_DIV(lq * q, h) + (lf[1] * nx + lf[2] * ny) * h;
+  const double q = fma(hu, nx, hv * ny) * ih;
+  const double lqh = fma(lf[1], hu, lf[2] * hv) * ih;
+  const double lhveln = lf[0] + lqh;
+  *lhu = fma(lf[1], q, fma(lhveln, nx, *lhu));
+  *lhv = fma(lf[2], q, fma(lhveln, ny, *lhv));
+  *lh = fma(-lqh, q, fma(fma(lf[1], nx, lf[2] * ny), h, *lh));
 }
 
 // wave-speed reverse: given la0, la1, adds to lul, lhl, lur, lhr
-SWE_HD void wavespeeds_rev(int ws, double ul, double hl, double ur, double hr, double la0, double la1, double* lul,
+SWE_HD void wavespeeds_rev(int ws, const WsFwd& f, double ul, double ur, double la0, double la1, double* lul,
                            double* lhl, double* lur, double* lhr) {
-  const double cl = SWE_SQRT(hl), cr = SWE_SQRT(hr);
   double lcl = 0., lcr = 0.;
   if (ws == 0) {
-    const double xl = fabs(ul) + cl, xr = fabs(ur) + cr;
     const double lap = la1 - la0;
-    if (dlt(xl, xr)) {  // smax picked the right side
+    if (dlt(fabs(ul) + f.cl, fabs(ur) + f.cr)) {  // smax picked the right side
       *lur += signbit(ur) ? -lap : lap;
       lcr += lap;
     } else {
@@ -41,14 +89,14 @@ SWE_HD void wavespeeds_rev(int ws, double ul, double hl, double ur, double hr, d
       lcl += lap;
     }
   } else if (ws == 1) {
-    if (dlt(ur - cr, ul - cl)) {
+    if (dlt(ur - f.cr, ul - f.cl)) {
       *lur += la0;
       lcr -= la0;
     } else {
       *lul += la0;
       lcl -= la0;
     }
-    if (dlt(ul + cl, ur + cr)) {
+    if (dlt(ul + f.cl, ur + f.cr)) {
       *lur += la1;
       lcr += la1;
     } else {
@@ -56,38 +104,36 @@ SWE_HD void wavespeeds_rev(int ws, double ul, double hl, double ur, double hr, d
       lcl += la1;
     }
   } else {
-    const double S = cl + cr;
-    const double uRoe = SWE_DIV(cl * ul + cl * ur, S);
-    const double cRoe = SWE_SQRT(0.5 * (hl + hr));
     double luRoe = 0., lcRoe = 0.;
-    if (dlt(uRoe - cRoe, ul - cl)) {
+    if (dlt(f.uRoe - f.cRoe, ul - f.cl)) {
       luRoe += la0;
       lcRoe -= la0;
     } else {
       *lul += la0;
       lcl -= la0;
     }
-    if (dlt(ur + cr, uRoe + cRoe)) {
+    if (dlt(ur + f.cr, f.uRoe + f.cRoe)) {
       luRoe += la1;
       lcRoe += la1;
     } else {
       *lur += la1;
       lcr += la1;
     }
-    if (cRoe > 0.) {
-      const double lm = SWE_DIV(0.5 * lcRoe, cRoe);
-      *lhl += 0.5 * lm;
-      *lhr += 0.5 * lm;
+    if (f.cRoe > 0.) {  // cRoe = sqrt((hl + hr) / 2)
+      const double lm = lcRoe * SWE_DIV(0.25, f.cRoe);
+      *lhl += lm;
+      *lhr += lm;
     }
-    const double lN = SWE_DIV(luRoe, S);
-    const double lS = -SWE_DIV(luRoe * uRoe, S);
-    lcl += lN * (ul + ur) + lS;
-    *lul += lN * cl;
-    *lur += lN * cl;
+    // uRoe = cl (ul + ur) / S, S = cl + cr
+    const double lN = luRoe * SWE_DIV(1., f.S);
+    const double lS = -lN * f.uRoe;
+    lcl = fma(lN, ul + ur, lcl + lS);
+    *lul = fma(lN, f.cl, *lul);
+    *lur = fma(lN, f.cl, *lur);
     lcr += lS;
   }
-  if (cl > 0.) *lhl += SWE_DIV(0.5 * lcl, cl);
-  if (cr > 0.) *lhr += SWE_DIV(0.5 * lcr, cr);
+  if (f.cl > 0.) *lhl = fma(lcl, SWE_DIV(0.5, f.cl), *lhl);
+  if (f.cr > 0.) *lhr = fma(lcr, SWE_DIV(0.5, f.cr), *lhr);
 }
 
 // Reverse of one interior edge's flux.  g: edge geometry; L, R: interface
@@ -103,148 +149,149 @@ SWE_HD void flux_reverse(int flux, int ws, const EdgeGeom& g, const SideState& L
   if (!dgtc(hl + hr, kMinCapture)) return;
   double lul = 0., lhl = 0., lur = 0., lhr = 0., lvl = 0., lvr = 0.;
   double lLu = 0., lLv = 0., lRu = 0., lRv = 0.;
+  const WsFwd f = ws_forward(ws, ul, hl, ur, hr);
   if (flux == 0) {
-    double a0, a1;
-    switch (ws) {
-      case 0: Rusanov::speeds(ul, hl, ur, hr, &a0, &a1); break;
-      case 1: Davis::speeds(ul, hl, ur, hr, &a0, &a1); break;
-      default: Einfeldt::speeds(ul, hl, ur, hr, &a0, &a1); break;
-    }
+    const double a0 = f.a0, a1 = f.a1;
     const double al = smin(0., a0);
     const double ar = smax(0., a1);
     if (!dgtc(ar - al, kMinCapture)) return;
+    const double ihl = is_wet(hl) ? SWE_DIV(1., hl) : 0.;
+    const double ihr = is_wet(hr) ? SWE_DIV(1., hr) : 0.;
     const double Ul[3] = {hl, hl * L.u, hl * L.v};
     const double Ur[3] = {hr, hr * R.u, hr * R.v};
     double Fl[3], Fr[3];
-    elem_flux(nx, ny, Ul[0], Ul[1], Ul[2], Fl);
-    elem_flux(nx, ny, Ur[0], Ur[1], Ur[2], Fr);
-    const double Dn = ar - al;
-    double F[3], lG[3];
+    elem_flux_fma(nx, ny, Ul[0], Ul[1], Ul[2], ihl, Fl);
+    elem_flux_fma(nx, ny, Ur[0], Ur[1], Ur[2], ihr, Fr);
+    const double iDn = SWE_DIV(1., ar - al);
+    const double alar = al * ar;
+    double lG[3], dU[3];
     double lDn = 0.;
+#pragma unroll
     for (int q = 0; q < 3; ++q) {
-      F[q] = SWE_DIV(ar * Fl[q] - al * Fr[q] + (al * ar) * (Ur[q] - Ul[q]), Dn);
-      lG[q] = SWE_DIV(lF[q], Dn);
-      lDn -= SWE_DIV(lF[q] * F[q], Dn);
+      dU[q] = Ur[q] - Ul[q];
+      const double F = fma(ar, Fl[q], fma(-al, Fr[q], alar * dU[q])) * iDn;
+      lG[q] = lF[q] * iDn;
+      lDn = fma(-lG[q], F, lDn);
     }
     double lar = lDn, lal = -lDn;
     double lFl[3], lFr[3], lUl[3], lUr[3];
+#pragma unroll
     for (int q = 0; q < 3; ++q) {
-      lar += lG[q] * (Fl[q] + al * (Ur[q] - Ul[q]));
-      lal += lG[q] * (-Fr[q] + ar * (Ur[q] - Ul[q]));
+      lar = fma(lG[q], fma(al, dU[q], Fl[q]), lar);
+      lal = fma(lG[q], fma(ar, dU[q], -Fr[q]), lal);
       lFl[q] = ar * lG[q];
       lFr[q] = -al * lG[q];
-      lUr[q] = (al * ar) * lG[q];
-      lUl[q] = -(al * ar) * lG[q];
+      lUr[q] = alar * lG[q];
+      lUl[q] = -lUr[q];
     }
-    elem_flux_rev(nx, ny, Ul[0], Ul[1], Ul[2], lFl, &lUl[0], &lUl[1], &lUl[2]);
-    elem_flux_rev(nx, ny, Ur[0], Ur[1], Ur[2], lFr, &lUr[0], &lUr[1], &lUr[2]);
+    elem_flux_rev(nx, ny, Ul[0], Ul[1], Ul[2], ihl, lFl, &lUl[0], &lUl[1], &lUl[2]);
+    elem_flux_rev(nx, ny, Ur[0], Ur[1], Ur[2], ihr, lFr, &lUr[0], &lUr[1], &lUr[2]);
     const double la0 = dlt(a0, 0.) ? lal : 0.;
     const double la1 = dlt(0., a1) ? lar : 0.;
-    wavespeeds_rev(ws, ul, hl, ur, hr, la0, la1, &lul, &lhl, &lur, &lhr);
-    lhl += lUl[0] + lUl[1] * L.u + lUl[2] * L.v;
-    lLu += lUl[1] * hl;
-    lLv += lUl[2] * hl;
-    lhr += lUr[0] + lUr[1] * R.u + lUr[2] * R.v;
-    lRu += lUr[1] * hr;
-    lRv += lUr[2] * hr;
+    wavespeeds_rev(ws, f, ul, ur, la0, la1, &lul, &lhl, &lur, &lhr);
+    lhl = fma(lUl[1], L.u, fma(lUl[2], L.v, lhl + lUl[0]));
+    lLu = fma(lUl[1], hl, lLu);
+    lLv = fma(lUl[2], hl, lLv);
+    lhr = fma(lUr[1], R.u, fma(lUr[2], R.v, lhr + lUr[0]));
+    lRu = fma(lUr[1], hr, lRu);
+    lRv = fma(lUr[2], hr, lRv);
   } else {
-    const double vl = L.u * tx + L.v * ty;
-    const double vr = R.u * tx + R.v * ty;
-    double al, ar;
-    switch (ws) {
-      case 0: Rusanov::speeds(ul, hl, ur, hr, &al, &ar); break;
-      case 1: Davis::speeds(ul, hl, ur, hr, &al, &ar); break;
-      default: Einfeldt::speeds(ul, hl, ur, hr, &al, &ar); break;
-    }
+    const double al = f.a0, ar = f.a1;
     const double A = ar - ur, B = al - ul;
-    double us = A * hr * ur - B * hl * ul + 0.5 * (hl * hl - hr * hr);
-    const double N = us;
+    // u* with the forward's operations (its sign picks the star side)
+    const double N = A * hr * ur - B * hl * ul + 0.5 * (hl * hl - hr * hr);
     const double D = hr * A - hl * B;
-    us = SWE_DIV(us, D);
-    (void)N;
+    const double us = SWE_DIV(N, D);
     double lus = 0., lA = 0., lB = 0., lar = 0., lal = 0.;
     if (!dgt0(us)) {
+      const double vr = fma(R.u, tx, R.v * ty);
+      const double ihr = is_wet(hr) ? SWE_DIV(1., hr) : 0.;
       const double Ur[3] = {hr, hr * R.u, hr * R.v};
-      const double uxs = vr * tx + us * ty;
-      const double vys = vr * nx + us * ny;
-      const double X = hr * A, Y = ar - us;
-      const double hs = SWE_DIV(X, Y);
+      const double uxs = fma(vr, tx, us * ty);
+      const double vys = fma(vr, nx, us * ny);
+      const double iY = SWE_DIV(1., ar - us);
+      const double hs = hr * A * iY;
       const double Us[3] = {hs, hs * uxs, hs * vys};
       const double sp = smax(0., ar);
       double lsp = 0., lUr[3], lUs[3];
+#pragma unroll
       for (int q = 0; q < 3; ++q) {
-        lsp += lF[q] * (Us[q] - Ur[q]);
+        lsp = fma(lF[q], Us[q] - Ur[q], lsp);
         lUs[q] = sp * lF[q];
-        lUr[q] = -sp * lF[q];
+        lUr[q] = -lUs[q];
       }
       if (dlt(0., ar)) lar += lsp;
-      elem_flux_rev(nx, ny, Ur[0], Ur[1], Ur[2], lF, &lUr[0], &lUr[1], &lUr[2]);
-      const double lhs = lUs[0] + lUs[1] * uxs + lUs[2] * vys;
+      elem_flux_rev(nx, ny, Ur[0], Ur[1], Ur[2], ihr, lF, &lUr[0], &lUr[1], &lUr[2]);
+      const double lhs = fma(lUs[1], uxs, fma(lUs[2], vys, lUs[0]));
       const double luxs = lUs[1] * hs, lvys = lUs[2] * hs;
-      const double lX = SWE_DIV(lhs, Y), lY = -SWE_DIV(lhs * hs, Y);
-      lhr += lX * A;
-      lA += lX * hr;
+      const double lX = lhs * iY, lY = -lX * hs;
+      lhr = fma(lX, A, lhr);
+      lA = fma(lX, hr, lA);
       lar += lY;
       lus -= lY;
-      lvr += luxs * tx + lvys * nx;
-      lus += luxs * ty + lvys * ny;
-      lhr += lUr[0] + lUr[1] * R.u + lUr[2] * R.v;
-      lRu += lUr[1] * hr;
-      lRv += lUr[2] * hr;
+      lvr = fma(luxs, tx, lvys * nx);
+      lus = fma(luxs, ty, fma(lvys, ny, lus));
+      lhr = fma(lUr[1], R.u, fma(lUr[2], R.v, lhr + lUr[0]));
+      lRu = fma(lUr[1], hr, lRu);
+      lRv = fma(lUr[2], hr, lRv);
     } else {
+      const double vl = fma(L.u, tx, L.v * ty);
+      const double ihl = is_wet(hl) ? SWE_DIV(1., hl) : 0.;
       const double Ul[3] = {hl, hl * L.u, hl * L.v};
-      const double uxs = vl * tx + us * ty;
-      const double vys = vl * nx + us * ny;
-      const double X = hl * B, Y = al - us;
-      const double hs = SWE_DIV(X, Y);
+      const double uxs = fma(vl, tx, us * ty);
+      const double vys = fma(vl, nx, us * ny);
+      const double iY = SWE_DIV(1., al - us);
+      const double hs = hl * B * iY;
       const double Us[3] = {hs, hs * uxs, hs * vys};
       const double sm = smin(0., al);
       double lsm = 0., lUl[3], lUs[3];
+#pragma unroll
       for (int q = 0; q < 3; ++q) {
-        lsm += lF[q] * (Us[q] - Ul[q]);
+        lsm = fma(lF[q], Us[q] - Ul[q], lsm);
         lUs[q] = sm * lF[q];
-        lUl[q] = -sm * lF[q];
+        lUl[q] = -lUs[q];
       }
       if (dlt(al, 0.)) lal += lsm;
-      elem_flux_rev(nx, ny, Ul[0], Ul[1], Ul[2], lF, &lUl[0], &lUl[1], &lUl[2]);
-      const double lhs = lUs[0] + lUs[1] * uxs + lUs[2] * vys;
+      elem_flux_rev(nx, ny, Ul[0], Ul[1], Ul[2], ihl, lF, &lUl[0], &lUl[1], &lUl[2]);
+      const double lhs = fma(lUs[1], uxs, fma(lUs[2], vys, lUs[0]));
       const double luxs = lUs[1] * hs, lvys = lUs[2] * hs;
-      const double lX = SWE_DIV(lhs, Y), lY = -SWE_DIV(lhs * hs, Y);
-      lhl += lX * B;
-      lB += lX * hl;
+      const double lX = lhs * iY, lY = -lX * hs;
+      lhl = fma(lX, B, lhl);
+      lB = fma(lX, hl, lB);
       lal += lY;
       lus -= lY;
-      lvl += luxs * tx + lvys * nx;
-      lus += luxs * ty + lvys * ny;
-      lhl += lUl[0] + lUl[1] * L.u + lUl[2] * L.v;
-      lLu += lUl[1] * hl;
-      lLv += lUl[2] * hl;
+      lvl = fma(luxs, tx, lvys * nx);
+      lus = fma(luxs, ty, fma(lvys, ny, lus));
+      lhl = fma(lUl[1], L.u, fma(lUl[2], L.v, lhl + lUl[0]));
+      lLu = fma(lUl[1], hl, lLu);
+      lLv = fma(lUl[2], hl, lLv);
     }
     // us = N / D
-    const double lN = SWE_DIV(lus, D);
-    const double lD = -SWE_DIV(lus * us, D);
-    lhr += lD * A;
-    lA += lD * hr;
-    lhl -= lD * B;
-    lB -= lD * hl;
-    lA += lN * hr * ur;
-    lhr += lN * A * ur;
-    lur += lN * A * hr;
-    lB -= lN * hl * ul;
-    lhl -= lN * B * ul;
-    lul -= lN * B * hl;
-    lhl += lN * hl;
-    lhr -= lN * hr;
+    const double lN = lus * SWE_DIV(1., D);
+    const double lD = -lN * us;
+    lhr = fma(lD, A, lhr);
+    lA = fma(lD, hr, lA);
+    lhl = fma(-lD, B, lhl);
+    lB = fma(-lD, hl, lB);
+    const double lNhr = lN * hr, lNhl = lN * hl;
+    lA = fma(lNhr, ur, lA);
+    lhr = fma(lN * A, ur, lhr);
+    lur = fma(lNhr, A, lur);
+    lB = fma(-lNhl, ul, lB);
+    lhl = fma(-lN * B, ul, lhl);
+    lul = fma(-lNhl, B, lul);
+    lhl += lNhl;
+    lhr -= lNhr;
     lar += lA;
     lur -= lA;
     lal += lB;
     lul -= lB;
-    wavespeeds_rev(ws, ul, hl, ur, hr, lal, lar, &lul, &lhl, &lur, &lhr);
+    wavespeeds_rev(ws, f, ul, ur, lal, lar, &lul, &lhl, &lur, &lhr);
   }
-  lLu += lul * nx + lvl * tx;
-  lLv += lul * ny + lvl * ty;
-  lRu += lur * nx + lvr * tx;
-  lRv += lur * ny + lvr * ty;
+  lLu = fma(lul, nx, fma(lvl, tx, lLu));
+  lLv = fma(lul, ny, fma(lvl, ty, lLv));
+  lRu = fma(lur, nx, fma(lvr, tx, lRu));
+  lRv = fma(lur, ny, fma(lvr, ty, lRv));
   lL[0] += lhl;
   lL[1] += lLu;
   lL[2] += lLv;

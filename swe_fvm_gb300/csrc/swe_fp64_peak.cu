@@ -168,7 +168,22 @@ __global__ void k_flux_adj_selftest(int flux, int ws, int n, unsigned long long 
     num = fmax(num, fabs(hand[k] - ref));
     den = fmax(den, fabs(ref));
   }
-  const double err = den > 0. ? num / den : num;
+  double err = den > 0. ? num / den : num;
+  // the reverse's own wave speeds must equal the forward plugin's bit for bit
+  {
+    const double ul = L.u * g.nx + L.v * g.ny, hl = L.w - g.b;
+    const double ur = R.u * g.nx + R.v * g.ny, hr = R.w - g.b;
+    const swe::WsFwd f = swe::ws_forward(ws, ul, hl, ur, hr);
+    double a0, a1;
+    switch (ws) {
+      case 0: swe::Rusanov::speeds(ul, hl, ur, hr, &a0, &a1); break;
+      case 1: swe::Davis::speeds(ul, hl, ur, hr, &a0, &a1); break;
+      default: swe::Einfeldt::speeds(ul, hl, ur, hr, &a0, &a1); break;
+    }
+    if (__double_as_longlong(a0) != __double_as_longlong(f.a0) ||
+        __double_as_longlong(a1) != __double_as_longlong(f.a1))
+      err = 1.;
+  }
   // exact max via integer atomics on the (non-negative) double bit pattern
   atomicMax((unsigned long long*)maxerr, (unsigned long long)__double_as_longlong(err));
 }

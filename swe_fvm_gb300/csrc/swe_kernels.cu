@@ -396,12 +396,15 @@ __global__ void __launch_bounds__(256) k_drain(DevMesh m, DevWork wk, const doub
 }
 
 // TimeDisc::RHS + the Shu-Osher combination + ConsAssigner.
-template <bool BATCH>
 // The output may be the same array as Wp or W0 (in-place stages): each thread
 // reads its own cell before writing it, so no pointer here is __restrict__.
+// STORE_N also writes the state before ConsAssigner to nst [3][C] (for the
+// adjoint's segment recompute).
+template <bool BATCH, bool STORE_N = false>
 __global__ void __launch_bounds__(256) k_update(DevMesh m, DevWork wk, const double* Wp, const double* Up,
                                                 const double* Vp, const double* W0, const double* U0,
-                                                const double* V0, double* Wo, double* Uo, double* Vo, Stage st) {
+                                                const double* V0, double* Wo, double* Uo, double* Vo, Stage st,
+                                                double* nst = nullptr) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= m.C) return;
   const int C = m.C;
@@ -446,6 +449,11 @@ __global__ void __launch_bounds__(256) k_update(DevMesh m, DevWork wk, const dou
     n0 = st.a * c00 + st.b * c10 + r0;
     n1 = st.a * c01 + st.b * c11 + r1;
     n2 = st.a * c02 + st.b * c12 + r2;
+  }
+  if (STORE_N) {
+    nst[i] = n0;
+    nst[C + i] = n1;
+    nst[2 * C + i] = n2;
   }
   double ow, ou, ov;
   cons_assign(b, n0, n1, n2, &ow, &ou, &ov);
@@ -710,6 +718,19 @@ cudaError_t Engine::step_timed(int scheme, int latch_mode, double* acc) {
   for (auto& row : ev)
     for (auto& x : row) cudaEventDestroy(x);
   return e;
+}
+
+cudaError_t Engine::update_only(const Stage& st, const double* const* in, const double* const* u0,
+                                double* const* out, double* nst) {
+  const int b = block_;
+  if (batched_)
+    k_update<true, true><<<nblocks(mesh_.C, b), b, 0, stream_>>>(mesh_, work_, in[0], in[1], in[2], u0[0], u0[1],
+                                                                 u0[2], out[0], out[1], out[2], st, nst);
+  else
+    k_update<false, true><<<nblocks(mesh_.C, b), b, 0, stream_>>>(mesh_, work_, in[0], in[1], in[2], u0[0], u0[1],
+                                                                  u0[2], out[0], out[1], out[2], st, nst);
+  ++launches_;
+  return cudaGetLastError();
 }
 
 cudaError_t Engine::stage_explicit(const Stage& st, const double* const* in, const double* const* u0,
