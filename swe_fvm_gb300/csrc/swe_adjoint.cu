@@ -560,9 +560,116 @@ __device__ void combo_points_to_nodes(const DevMesh& m, AdjWork& aw, int c, int 
   }
 }
 
-// Reverse of the reconstruction of cell i.  PASS 1: dry and fully-wet cells;
-// PASS 2: partially-wet cells only.
-template <int PASS>
+// Forward-only part of a partially-wet cell's reverse: the PartWet2 plane (or
+// PartWet1 level) with its derivatives, and where the PartWet2 node maximum
+// w23 came from.  It reads no adjoint, so it runs beside R1-R3.
+__device__ void pw_jacobian(const DevMesh& m, const DevWork& wk, const AdjWork& aw, const double* W, int i,
+                            PwJac* out) {
+  const int C = m.C;
+  const double w = W[i];
+  const Pw2Rec& r = m.pw2[i];
+  const double w23 = order_val(wk.maxwp[r.lo]);
+  typedef Dual<5> D5;  // PartWet2 over (w, w23, z_lo, z_mid, z_hi)
+  D5 zc[3];
+  for (int k = 0; k < 3; ++k) zc[k] = D5(m.zn[k * C + i]);
+  const D5 zl = D5::var(r.p[0][2], 2), zm = D5::var(r.p[1][2], 3), zh = D5::var(r.p[2][2], 4);
+  for (int s = 0; s < 3; ++s) zc[r.sk[s]] = (s == 0) ? zl : (s == 1 ? zm : zh);
+  const double k3 = 1. / 3.;
+  D5 bcd = zc[0] * k3 + zc[1] * k3 + zc[2] * k3;
+  bcd.v = m.bc[i];  // the forward's centroid bathymetry
+  D5 w0D, gxD, gyD;
+  PwJac J;
+  J.plane = partwet2_t(r, D5::var(w, 0), D5::var(w23, 1), zl, zm, zh, bcd, &w0D, &gxD, &gyD) ? 1 : 0;
+  J.route = 0;
+  J.target = r.lo;
+  J.mask = -1;
+  for (int q = 0; q < 4; ++q) J.rc[q] = 0.;
+  if (!J.plane) {
+    // PartWet1 level: dual over (w, z0, z1, z2)
+    typedef Dual<4> D;
+    const double lvl = wk.pwrec[i];
+    const D y = partwet1_t(D::var(w, 0), D::var(m.zn[i], 1), D::var(m.zn[C + i], 2), D::var(m.zn[2 * C + i], 3), lvl);
+    J.w0 = lvl;
+    J.gx = 0.;
+    J.gy = 0.;
+    for (int q = 0; q < 5; ++q) {
+      J.jw0[q] = q < 4 ? y.d[q] : 0.;
+      J.jgx[q] = 0.;
+      J.jgy[q] = 0.;
+    }
+    *out = J;
+    return;
+  }
+  J.w0 = w0D.v;
+  J.gx = gxD.v;
+  J.gy = gyD.v;
+  for (int q = 0; q < 5; ++q) {
+    J.jw0[q] = w0D.d[q];
+    J.jgx[q] = gxD.d[q];
+    J.jgy[q] = gyD.d[q];
+  }
+  // w23 = max over the cells around the lowest node of their pass-1 value
+  const int nd = r.lo;
+  int best = -1, bestk = 0;
+  for (int q = aw.node_ptr[nd]; q < aw.node_ptr[nd + 1]; ++q) {
+    const int c = aw.node_cells[q] >> 2, kn = aw.node_cells[q] & 3;
+    if (pass1_node_value(m, W, c, kn, wk.pwrec) == w23) {
+      best = c;
+      bestk = kn;
+      break;
+    }
+  }
+  if (best >= 0) {
+    const P1 pc = pass1(m, W, best, wk.pwrec);
+    const double zc_ = m.zn[bestk * C + best];
+    J.route = 0;
+    J.target = cnode(m, best, bestk);
+    if (pc.type == 0) {
+      // dry plane value at the node: a function of bathymetry only
+      typedef Dual<3> E;
+      const Pw2Rec& rb = m.pw2[best];
+      E z0 = E::var(m.zn[best], 0), z1 = E::var(m.zn[C + best], 1), z2 = E::var(m.zn[2 * C + best], 2);
+      E sxd, syd;
+      plane_gradient_t(E(rb.dnode[0][0]), E(rb.dnode[0][1]), z0, E(rb.dnode[1][0]), E(rb.dnode[1][1]), z1,
+                       E(rb.dnode[2][0]), E(rb.dnode[2][1]), z2, &sxd, &syd);
+      E bcb = z0 * k3 + z1 * k3 + z2 * k3;
+      E a = bcb + (sxd * rb.dnode[bestk][0] + syd * rb.dnode[bestk][1]);
+      if (dge0(a.v - zc_)) {
+        J.route = 1;
+        J.target = best;
+        for (int q = 0; q < 3; ++q) J.rc[q] = a.d[q];
+      }
+    } else {
+      double off_n = 0.;
+      if (pc.type == 2 && pc.kept) off_n = m.combo[((size_t)best * 8 + pc.mask) * kComboStride + 8 + bestk];
+      if (dge0((pc.w0 + off_n) - zc_)) {
+        J.target = best;
+        if (pc.type == 2) {
+          // the fully-wet cell's level, and its vertex offset a_k = g . (P_k - T)
+          // moving with the plane's point z
+          J.route = 2;
+          if (pc.kept) {
+            const Pw2Rec& rb = m.pw2[best];
+            double px[3], py[3];
+            combo_plane_points(m, best, pc.mask, px, py);
+            plane_points_adjoint(px, py, rb.dnode[bestk][0], rb.dnode[bestk][1], J.rc);
+            J.mask = pc.mask;
+          }
+        } else {
+          typedef Dual<4> F4;
+          const F4 y = partwet1_t(F4::var(W[best], 0), F4::var(m.zn[best], 1), F4::var(m.zn[C + best], 2),
+                                  F4::var(m.zn[2 * C + best], 3), pc.w0);
+          J.route = 3;
+          for (int q = 0; q < 4; ++q) J.rc[q] = y.d[q];
+        }
+      }
+    }
+  }
+  *out = J;
+}
+
+// Reverse of the reconstruction of cell i; partially-wet cells contract the
+// Jacobians pw_jacobian stored for them.
 __device__ void adj_recon_cell(const DevMesh& m, const DevWork& wk, AdjWork aw, const double* W, const double* U,
                                const double* V, int i, int batched) {
   const int C = m.C;
@@ -581,47 +688,38 @@ __device__ void adj_recon_cell(const DevMesh& m, const DevWork& wk, AdjWork aw, 
     }
   }
   const P1 p = pass1(m, W, i, wk.pwrec);
-  if ((PASS == 1 && p.type == 1) || (PASS == 2 && p.type != 1)) return;
-  // forward description of the final interface values: level w0 + off_k, velocity, slope
-  double w0 = w, gx = 0., gy = 0., off[3] = {0., 0., 0.};
-  double u0 = u, v0 = v;
-  bool pw2_plane = false;
-  double w23 = 0.;
-  int lo_node = -1;
-  typedef Dual<5> D5;  // PartWet2 over (w, w23, z_lo, z_mid, z_hi)
-  D5 w0D, gxD, gyD;
-  if (PASS == 1 && p.type == 0) {
+  if (p.type == 0) {
     const double* dr = m.dry + (size_t)i * kDryStride;
-    // interface values (dew_k, 0, 0) and slope (sx, sy): all bathymetry
+    // interface values (dew_k, 0, 0) and slope (sx, sy) are functions of the
+    // cell's node z: dual over z0..z2
+    typedef Dual<3> D;
+    D z0 = D::var(m.zn[i], 0), z1 = D::var(m.zn[C + i], 1), z2 = D::var(m.zn[2 * C + i], 2);
+    const Pw2Rec& r = m.pw2[i];
+    // node positions relative to the centroid (slopes depend on differences only)
+    D sxd, syd;
+    plane_gradient_t(D(r.dnode[0][0]), D(r.dnode[0][1]), z0, D(r.dnode[1][0]), D(r.dnode[1][1]), z1,
+                     D(r.dnode[2][0]), D(r.dnode[2][1]), z2, &sxd, &syd);
+    const double k3 = 1. / 3.;
+    const D bcd = z0 * k3 + z1 * k3 + z2 * k3;
+    double lz3[3] = {0., 0., 0.};
     for (int k = 0; k < 3; ++k) {
       const int slot = k * C + i;
       double law, lu0, lv0, lgx, lgy, lze;
       slot_reverse(m.ze[slot], dr[3 + k], 0., 0., cor, aw.lew[slot], aw.leu[slot], aw.lev[slot], aw.lsx[slot],
                    aw.lsy[slot], &law, &lu0, &lv0, &lgx, &lgy, &lze);
-      lze += aw.lze[slot];
-      // dew_k and (sx, sy) as functions of the cell's node z: dual over z0..z2
-      typedef Dual<3> D;
-      D z0 = D::var(m.zn[i], 0), z1 = D::var(m.zn[C + i], 1), z2 = D::var(m.zn[2 * C + i], 2);
-      const Pw2Rec& r = m.pw2[i];
-      // node positions in cell order from dnode (P_k - T) and T: recover P_k = T + dnode_k
-      // (T is never needed: slopes depend on differences only)
-      D sxd, syd;
-      plane_gradient_t(D(r.dnode[0][0]), D(r.dnode[0][1]), z0, D(r.dnode[1][0]), D(r.dnode[1][1]), z1,
-                       D(r.dnode[2][0]), D(r.dnode[2][1]), z2, &sxd, &syd);
-      const double k3 = 1. / 3.;
-      D bcd = z0 * k3 + z1 * k3 + z2 * k3;
-      D e0v = bcd + (sxd * r.dedge[k][0] + syd * r.dedge[k][1]);
-      double lz3[3];
-      for (int q = 0; q < 3; ++q) lz3[q] = law * e0v.d[q] + lgx * sxd.d[q] + lgy * syd.d[q];
-      for (int q = 0; q < 3; ++q)
-        if (lz3[q] != 0.) atomicAdd(aw.lz + cnode(m, i, q), lz3[q]);
-      lam_edge_z(m, aw, i, k, lze);
+      const D e0v = bcd + (sxd * r.dedge[k][0] + syd * r.dedge[k][1]);
+      for (int q = 0; q < 3; ++q) lz3[q] = fma(law, e0v.d[q], fma(lgx, sxd.d[q], fma(lgy, syd.d[q], lz3[q])));
+      lam_edge_z(m, aw, i, k, lze + aw.lze[slot]);
     }
+    for (int q = 0; q < 3; ++q)
+      if (lz3[q] != 0.) atomicAdd(aw.lz + cnode(m, i, q), lz3[q]);
     lam_cell_z(m, aw, i, lbc);
     return;
   }
-  if (PASS == 1) {
-    w0 = w;
+  // forward description of the final interface values: level w0 + off_k, velocity, slope
+  double w0 = w, gx = 0., gy = 0., off[3] = {0., 0., 0.};
+  const PwJac* J = nullptr;
+  if (p.type == 2) {
     if (p.kept) {
       const double* rec = m.combo + ((size_t)i * 8 + p.mask) * kComboStride;
       gx = rec[0];
@@ -629,26 +727,13 @@ __device__ void adj_recon_cell(const DevMesh& m, const DevWork& wk, AdjWork aw, 
       for (int k = 0; k < 3; ++k) off[k] = rec[5 + k];
     }
   } else {
-    // partially wet: PartWet2 with the pass-1 maxima, else PartWet1; the dual
-    // evaluation gives the forward values bit for bit and their derivatives
-    const Pw2Rec& r = m.pw2[i];
-    lo_node = r.lo;
-    w23 = order_val(wk.maxwp[r.lo]);
-    D5 zc[3];
-    for (int k = 0; k < 3; ++k) zc[k] = D5(m.zn[k * C + i]);
-    const D5 zl = D5::var(r.p[0][2], 2), zm = D5::var(r.p[1][2], 3), zh = D5::var(r.p[2][2], 4);
-    for (int s = 0; s < 3; ++s) zc[r.sk[s]] = (s == 0) ? zl : (s == 1 ? zm : zh);
-    const double k3 = 1. / 3.;
-    D5 bcd = zc[0] * k3 + zc[1] * k3 + zc[2] * k3;
-    bcd.v = m.bc[i];  // the forward's centroid bathymetry
-    pw2_plane = partwet2_t(r, D5::var(w, 0), D5::var(w23, 1), zl, zm, zh, bcd, &w0D, &gxD, &gyD);
-    if (pw2_plane) {
-      w0 = w0D.v;
-      gx = gxD.v;
-      gy = gyD.v;
+    J = aw.pwjac + i;
+    w0 = J->w0;
+    if (J->plane) {
+      const Pw2Rec& r = m.pw2[i];
+      gx = J->gx;
+      gy = J->gy;
       for (int k = 0; k < 3; ++k) off[k] = gx * r.dedge[k][0] + gy * r.dedge[k][1];
-    } else {
-      w0 = p.w0;
     }
   }
   // slot reverses
@@ -656,7 +741,7 @@ __device__ void adj_recon_cell(const DevMesh& m, const DevWork& wk, AdjWork aw, 
   for (int k = 0; k < 3; ++k) {
     const int slot = k * C + i;
     double law, lu0, lv0, lgxk, lgyk, lze;
-    slot_reverse(m.ze[slot], w0 + off[k], u0, v0, cor, aw.lew[slot], aw.leu[slot], aw.lev[slot], aw.lsx[slot],
+    slot_reverse(m.ze[slot], w0 + off[k], u, v, cor, aw.lew[slot], aw.leu[slot], aw.lev[slot], aw.lsx[slot],
                  aw.lsy[slot], &law, &lu0, &lv0, &lgxk, &lgyk, &lze);
     lw0 += law;
     loff[k] = law;
@@ -666,109 +751,62 @@ __device__ void adj_recon_cell(const DevMesh& m, const DevWork& wk, AdjWork aw, 
     lgy += lgyk;
     lam_edge_z(m, aw, i, k, lze + aw.lze[slot]);
   }
-  if (PASS == 1) {
+  if (p.type == 2) {
     lw_i += lw0;
     if (p.kept) {
-      // the combination plane through neighbour centroids / edge centres
-      const Pw2Rec& r = m.pw2[i];
+      // the combination plane through neighbour centroids / edge centres:
       // off_k = g0 dEx + g1 dEy
+      const Pw2Rec& r = m.pw2[i];
       double lg0 = lgx, lg1 = lgy;
       for (int k = 0; k < 3; ++k) {
-        lg0 += loff[k] * r.dedge[k][0];
-        lg1 += loff[k] * r.dedge[k][1];
+        lg0 = fma(loff[k], r.dedge[k][0], lg0);
+        lg1 = fma(loff[k], r.dedge[k][1], lg1);
       }
       double px[3], py[3], lp[3];
       combo_plane_points(m, i, p.mask, px, py);
       plane_points_adjoint(px, py, lg0, lg1, lp);
       combo_points_to_nodes(m, aw, i, p.mask, lp);
     }
+  } else if (!J->plane) {
+    // PartWet1 level over (w, z0, z1, z2)
+    lw_i = fma(lw0, J->jw0[0], lw_i);
+    for (int q = 0; q < 3; ++q)
+      if (J->jw0[1 + q] != 0.) atomicAdd(aw.lz + cnode(m, i, q), lw0 * J->jw0[1 + q]);
   } else {
     const Pw2Rec& r = m.pw2[i];
-    int sorted_local[3] = {r.sk[0], r.sk[1], r.sk[2]};
-    if (pw2_plane) {
-      const double k3 = 1. / 3.;
-      const D5& w0d = w0D;
-      const D5& gxd = gxD;
-      const D5& gyd = gyD;
-      double lg0 = lgx, lg1 = lgy;
-      for (int k = 0; k < 3; ++k) {
-        lg0 += loff[k] * r.dedge[k][0];
-        lg1 += loff[k] * r.dedge[k][1];
-      }
-      double g[5];
-      for (int q = 0; q < 5; ++q) g[q] = lw0 * w0d.d[q] + lg0 * gxd.d[q] + lg1 * gyd.d[q];
-      lw_i += g[0];
-      // node z of the sorted vertices
-      for (int s = 0; s < 3; ++s)
-        if (g[2 + s] != 0.) atomicAdd(aw.lz + cnode(m, i, sorted_local[s]), g[2 + s]);
-      // w23 = max over the cells around the lowest node of their pass-1 value
-      if (g[1] != 0.) {
-        const int nd = lo_node;
-        int best = -1, bestk = 0;
-        for (int q = aw.node_ptr[nd]; q < aw.node_ptr[nd + 1]; ++q) {
-          const int c = aw.node_cells[q] >> 2, kn = aw.node_cells[q] & 3;
-          const double val_c = pass1_node_value(m, W, c, kn, wk.pwrec);
-          if (val_c == w23) {
-            best = c;
-            bestk = kn;
-            break;
+    double lg0 = lgx, lg1 = lgy;
+    for (int k = 0; k < 3; ++k) {
+      lg0 = fma(loff[k], r.dedge[k][0], lg0);
+      lg1 = fma(loff[k], r.dedge[k][1], lg1);
+    }
+    double g[5];
+    for (int q = 0; q < 5; ++q) g[q] = fma(lw0, J->jw0[q], fma(lg0, J->jgx[q], lg1 * J->jgy[q]));
+    lw_i += g[0];
+    // node z of the sorted vertices
+    for (int s = 0; s < 3; ++s)
+      if (g[2 + s] != 0.) atomicAdd(aw.lz + cnode(m, i, r.sk[s]), g[2 + s]);
+    // w23 through the cell that supplied the node maximum
+    const double g1 = g[1];
+    if (g1 != 0.) {
+      const int t = J->target;
+      switch (J->route) {
+        case 0: atomicAdd(aw.lz + t, g1); break;
+        case 1:
+          for (int q = 0; q < 3; ++q) atomicAdd(aw.lz + cnode(m, t, q), g1 * J->rc[q]);
+          break;
+        case 2:
+          atomicAdd(aw.lscatter + t, g1);
+          if (J->mask >= 0) {
+            const double lp[3] = {g1 * J->rc[0], g1 * J->rc[1], g1 * J->rc[2]};
+            combo_points_to_nodes(m, aw, t, J->mask, lp);
           }
-        }
-        if (best < 0) {
-          atomicAdd(aw.lz + nd, g[1]);  // the maximum is the node bathymetry itself
-        } else {
-          const P1 pc = pass1(m, W, best, wk.pwrec);
-          const double zc_ = m.zn[bestk * C + best];
-          if (pc.type == 0) {
-            // dry plane value at the node: a function of bathymetry only
-            typedef Dual<3> E;
-            const Pw2Rec& rb = m.pw2[best];
-            E z0 = E::var(m.zn[best], 0), z1 = E::var(m.zn[C + best], 1), z2 = E::var(m.zn[2 * C + best], 2);
-            E sxd, syd;
-            plane_gradient_t(E(rb.dnode[0][0]), E(rb.dnode[0][1]), z0, E(rb.dnode[1][0]), E(rb.dnode[1][1]), z1,
-                             E(rb.dnode[2][0]), E(rb.dnode[2][1]), z2, &sxd, &syd);
-            E bcb = z0 * k3 + z1 * k3 + z2 * k3;
-            E a = bcb + (sxd * rb.dnode[bestk][0] + syd * rb.dnode[bestk][1]);
-            if (dge0(a.v - zc_)) {
-              for (int q = 0; q < 3; ++q) atomicAdd(aw.lz + cnode(m, best, q), g[1] * a.d[q]);
-            } else {
-              atomicAdd(aw.lz + cnode(m, best, bestk), g[1]);
-            }
-          } else {
-            double off_n = 0.;
-            if (pc.type == 2 && pc.kept) off_n = m.combo[((size_t)best * 8 + pc.mask) * kComboStride + 8 + bestk];
-            const double a = pc.w0 + off_n;
-            if (!dge0(a - zc_)) {
-              atomicAdd(aw.lz + cnode(m, best, bestk), g[1]);
-            } else if (pc.type == 2) {
-              atomicAdd(aw.lscatter + best, g[1]);  // the fully-wet cell's level
-              if (pc.kept) {
-                // its vertex offset a_k = g . (P_k - T) moves with the plane's point z
-                const Pw2Rec& rb = m.pw2[best];
-                double px[3], py[3], lp[3];
-                combo_plane_points(m, best, pc.mask, px, py);
-                plane_points_adjoint(px, py, g[1] * rb.dnode[bestk][0], g[1] * rb.dnode[bestk][1], lp);
-                combo_points_to_nodes(m, aw, best, pc.mask, lp);
-              }
-            } else {
-              typedef Dual<4> F4;
-              F4 wb = F4::var(W[best], 0);
-              F4 y = partwet1_t(wb, F4::var(m.zn[best], 1), F4::var(m.zn[C + best], 2), F4::var(m.zn[2 * C + best], 3),
-                                pc.w0);
-              atomicAdd(aw.lscatter + best, g[1] * y.d[0]);
-              for (int q = 0; q < 3; ++q)
-                if (y.d[1 + q] != 0.) atomicAdd(aw.lz + cnode(m, best, q), g[1] * y.d[1 + q]);
-            }
-          }
-        }
+          break;
+        default:
+          atomicAdd(aw.lscatter + t, g1 * J->rc[0]);
+          for (int q = 0; q < 3; ++q)
+            if (J->rc[1 + q] != 0.) atomicAdd(aw.lz + cnode(m, t, q), g1 * J->rc[1 + q]);
+          break;
       }
-    } else {
-      // PartWet1 level: dual over (w, z0, z1, z2)
-      typedef Dual<4> D;
-      D y = partwet1_t(D::var(w, 0), D::var(m.zn[i], 1), D::var(m.zn[C + i], 2), D::var(m.zn[2 * C + i], 3), p.w0);
-      lw_i += lw0 * y.d[0];
-      for (int q = 0; q < 3; ++q)
-        if (y.d[1 + q] != 0.) atomicAdd(aw.lz + cnode(m, i, q), lw0 * y.d[1 + q]);
     }
   }
   aw.lamp[i] += lw_i;
@@ -780,16 +818,17 @@ __device__ void adj_recon_cell(const DevMesh& m, const DevWork& wk, AdjWork aw, 
 __global__ void __launch_bounds__(256) k_adj_recon(DevMesh m, DevWork wk, AdjWork aw, const double* W,
                                                    const double* U, const double* V, int batched) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < m.C) adj_recon_cell<1>(m, wk, aw, W, U, V, i, batched);
+  if (i < m.C) adj_recon_cell(m, wk, aw, W, U, V, i, batched);
 }
 
-// partially-wet cells of the stage (the list pass 1 of the forward wrote)
-// (one warp per block: the few listed cells spread over many SMs)
-__global__ void __launch_bounds__(32) k_adj_recon_pw(DevMesh m, DevWork wk, AdjWork aw, const double* W,
-                                                     const double* U, const double* V, int batched) {
+// Jacobians of the stage's partially-wet cells (the list pass 1 of the forward
+// wrote), one warp per block so that the few listed cells spread over the SMs
+__global__ void __launch_bounds__(32) k_pw_jacobian(DevMesh m, DevWork wk, AdjWork aw, const double* W) {
   const int n = min(*wk.pwcount, m.C);
-  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x)
-    adj_recon_cell<2>(m, wk, aw, W, U, V, wk.pwlist[q], batched);
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+    const int i = wk.pwlist[q];
+    pw_jacobian(m, wk, aw, W, i, aw.pwjac + i);
+  }
 }
 
 }  // namespace
@@ -852,6 +891,7 @@ std::string Engine::adjoint_init() {
   A(w.lew, 3 * C); A(w.leu, 3 * C); A(w.lev, 3 * C); A(w.lsx, 3 * C); A(w.lsy, 3 * C); A(w.lze, 3 * C);
   A(w.lF0, 3 * C); A(w.lF1, 3 * C); A(w.lF2, 3 * C); A(w.lF0d, 3 * C); A(w.ldtk, 3 * C); A(w.lhwall, 3 * C);
   A(w.lbc, C); A(w.lscatter, C); A(w.lz, N);
+  w.pwjac = a->alloc<PwJac>(C);
   w.route = a->alloc<unsigned char>(3 * C);
   ok = ok && w.route;
   // twin slots, node -> cells, edge nodes (host, from the instance's topology)
@@ -1152,6 +1192,14 @@ cudaError_t Engine::adjoint_stage_reverse_stored(const Stage& st, const double* 
                                                  AdjWork& aw, const DevWork& wk, const double* nst) {
   const int b = 256;
   const int gc = (mesh_.C + b - 1) / b, ge = (mesh_.E + b - 1) / b;
+  // the partially-wet cells' Jacobians need no adjoint: a side stream
+  // computes them while R1-R3 run
+  AdjointState& a = *adj_;
+  cudaEventRecord(a.ev_fork, stream_);
+  cudaStreamWaitEvent(a.side, a.ev_fork, 0);
+  const int gpw = std::max(1, std::min((mesh_.C + 31) / 32, 152 * 16));
+  k_pw_jacobian<<<gpw, 32, 0, a.side>>>(mesh_, wk, aw, in[0]);
+  cudaEventRecord(a.ev_join, a.side);
   k_adj_update<<<gc, b, 0, stream_>>>(mesh_, wk, aw, in[0], in[1], in[2], u0[0], u0[1], u0[2], nst, st, batched_);
   k_adj_drain<<<gc, b, 0, stream_>>>(mesh_, wk, aw, in[0]);
   switch (flux_ * 3 + ws_) {
@@ -1162,15 +1210,8 @@ cudaError_t Engine::adjoint_stage_reverse_stored(const Stage& st, const double* 
     case 4: k_adj_flux<1, 1><<<ge, b, 0, stream_>>>(mesh_, wk, aw, in[0]); break;
     default: k_adj_flux<1, 2><<<ge, b, 0, stream_>>>(mesh_, wk, aw, in[0]); break;
   }
-  // partially-wet cells on a side stream, overlapping the rest of the reconstruction reverse
-  AdjointState& a = *adj_;
-  cudaEventRecord(a.ev_fork, stream_);
-  cudaStreamWaitEvent(a.side, a.ev_fork, 0);
-  const int gpw = std::max(1, std::min((mesh_.C + 31) / 32, 152 * 16));
-  k_adj_recon_pw<<<gpw, 32, 0, a.side>>>(mesh_, wk, aw, in[0], in[1], in[2], batched_);
-  cudaEventRecord(a.ev_join, a.side);
-  k_adj_recon<<<gc, b, 0, stream_>>>(mesh_, wk, aw, in[0], in[1], in[2], batched_);
   cudaStreamWaitEvent(stream_, a.ev_join, 0);
+  k_adj_recon<<<gc, b, 0, stream_>>>(mesh_, wk, aw, in[0], in[1], in[2], batched_);
   launches_ += 5;
   return cudaGetLastError();
 }

@@ -5,6 +5,20 @@
 
 namespace swe {
 
+// Forward-only part of a partially-wet cell's reconstruction reverse.
+struct PwJac {
+  double w0, gx, gy;  // the forward plane (level, slope)
+  // plane: d(w0, gx, gy) / d(w, w23, z_lo, z_mid, z_hi); PartWet1 level:
+  // jw0[0..3] = d level / d(w, z0, z1, z2)
+  double jw0[5], jgx[5], jgy[5];
+  // where w23 (the PartWet2 node maximum) came from: route 0 node `target`;
+  // 1 dry cell `target` (rc[0..2] to its nodes); 2 fully-wet cell `target`
+  // (its level; rc[0..2] plane-point weights of combination `mask` when
+  // mask >= 0); 3 PartWet1 cell `target` (rc[0] its level, rc[1..3] its nodes)
+  double rc[4];
+  int plane, route, target, mask;
+};
+
 struct AdjWork {
   double* lam;   // [3][C] adjoint of the stage output (w, u, v)
   double* lamp;  // [3][C] adjoint of the stage input, accumulated
@@ -22,6 +36,7 @@ struct AdjWork {
   const int* node_ptr;                        // [N+1] cells around each node (CSR)
   const int* node_cells;                      // (cell << 2) | local node index
   const int* edge_nodes;                      // [2E] global node ids of each edge
+  PwJac* pwjac;                               // [C] partially-wet cells' Jacobians
 };
 
 }  // namespace swe
