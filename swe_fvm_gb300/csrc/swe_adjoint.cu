@@ -138,8 +138,8 @@ __global__ void __launch_bounds__(256) k_adj_update(DevMesh m, DevWork wk, AdjWo
       r1 -= q * wk.sx[slot] * h_ek;
       r2 -= q * wk.sy[slot] * h_ek;
       const double p = 0.5 * h_ek * h_ek;
-      r1 += dtk * (m.cnx[slot] * c_ek * p);
-      r2 += dtk * (m.cny[slot] * c_ek * p);
+      r1 += dtk * (m.cnxc[slot] * p);
+      r2 += dtk * (m.cnyc[slot] * p);
     }
     const double c00 = h0, c01 = h0 * U0[i], c02 = h0 * V0[i];
     if (st.first) {
@@ -208,7 +208,7 @@ __global__ void __launch_bounds__(256) k_adj_update(DevMesh m, DevWork wk, AdjWo
     const double dtk = dtk_[k];
     const double sc = out ? c_ek : -c_ek;  // sgn c_ek
     const double s = dtk * sc;
-    const double nxc = m.cnx[slot] * c_ek, nyc = m.cny[slot] * c_ek;
+    const double nxc = m.cnxc[slot], nyc = m.cnyc[slot];
     const double lpn = fma(ln1, nxc, ln2 * nyc);
     const double ls = -fma(ln0, F0, fma(ln1, F1, ln2 * F2));
     const double ldtk = fma(ls, sc, lpn * p);

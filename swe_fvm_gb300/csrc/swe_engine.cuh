@@ -55,8 +55,8 @@ struct DevMesh {
   const double* zn;           // [3][C] node z
   const double* ze;           // [3][C] edge-centre z
   const double* cek;          // [3][C] L(e_k) / A
-  const double* cnx;          // [3][C] outward normal of edge k
-  const double* cny;          // [3][C]
+  const double* cnxc;         // [3][C] outward normal of edge k times L_k / A (x)
+  const double* cnyc;         // [3][C] (y)
   const double* dry;          // [C][8] dry-cell node/edge values and slope
   const double* combo;        // [C][8][12] full-wet plane records
   const double* pw1;          // [C][12]
@@ -213,6 +213,11 @@ class Engine {
   cudaStream_t own_stream_ = nullptr;
   int flux_ = 1, ws_ = 2, block_ = 256;
   bool batched_ = false;
+  bool cor0_ = true;  // every instance has cor = 0: no Coriolis arithmetic in the reconstruction
+  void launch_recon1(const double* W, const double* U, const double* V, int latch_mode);
+  void launch_recon2(const double* W, const double* U, const double* V);
+  void launch_update(const Stage& st, const double* const* in, const double* const* u0, double* const* out,
+                     double* nst);
   int64_t launches_ = 0;
   cudaGraphExec_t graphs_[3][3] = {};
   AdjointState* adj_ = nullptr;
@@ -224,7 +229,7 @@ struct HostImage {
   int C, E, N, I;
   std::vector<int> cnode, cnbr, cedge, cinst, eown, enb, eslotl, eslotr, einst, inst_cell_begin;
   std::vector<unsigned char> cown;
-  std::vector<double> bc, fwthr, area, zn, ze, cek, cnx, cny, dry, combo, pw1, enx, eny, etx, ety, ezm, elmin, nz,
+  std::vector<double> bc, fwthr, area, zn, ze, cek, cnxc, cnyc, dry, combo, pw1, enx, eny, etx, ety, ezm, elmin, nz,
       inst_cfl, inst_cor;
   std::vector<Pw2Rec> pw2;
   void resize(int C_, int E_, int N_, int I_);

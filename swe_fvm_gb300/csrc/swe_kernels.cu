@@ -53,6 +53,20 @@ __device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }
 // UpdateInterfaceValues for one edge slot (src/SpaceDisc.cpp:24-29): AtPoint
 // value (w, u, v) already dry-checked, through PrimAssigner with the edge
 // bathymetry, plus the source gradient and Coriolis term.
+// Source gradient plus the Coriolis term, (gx, gy) + cor (-v, u).  COR0 (cor
+// is +-0 for every instance): x + (+-0) is x unless x is itself a zero, and
+// then -0 only if both are -0, so the same bits come from integer operations.
+// (A non-finite velocity would give NaN through the arithmetic; its state is
+// already non-finite and reported by the update kernel.)
+__device__ __forceinline__ double add_zero_product(double x, double c, double v) {
+  const unsigned long long ux = (unsigned long long)dbits(x);
+  if ((ux << 1) != 0ull) return x;
+  const unsigned long long uc = (unsigned long long)dbits(c);
+  const unsigned long long uv = (unsigned long long)dbits(v);
+  return dfrom((long long)(ux & (uc ^ uv) & 0x8000000000000000ull));
+}
+
+template <bool COR0>
 __device__ __forceinline__ void write_slot(const DevWork& wk, int slot, double be, double w, double u, double v,
                                            double gx, double gy, double cor) {
   double ow, ou, ov;
@@ -61,8 +75,14 @@ __device__ __forceinline__ void write_slot(const DevWork& wk, int slot, double b
   wk.eu[slot] = ou;
   wk.ev[slot] = ov;
   double sx = gx, sy = gy;
-  sx += cor * (-ov);
-  sy += cor * ou;
+  if (COR0) {
+    const double nov = dfrom(dbits(ov) ^ (long long)0x8000000000000000ull);
+    sx = add_zero_product(gx, cor, nov);
+    sy = add_zero_product(gy, cor, ou);
+  } else {
+    sx += cor * (-ov);
+    sy += cor * ou;
+  }
   wk.sx[slot] = sx;
   wk.sy[slot] = sy;
 }
@@ -82,7 +102,7 @@ __device__ __forceinline__ bool at_point_wet(double w0, double off, double z, do
 __device__ __forceinline__ void node_max(const DevWork& wk, int node, double val, double z) {
   // max_wp starts at the node z and every AtPoint value is >= z, so values
   // equal to z cannot raise it.
-  if (val != z) atomicMax(wk.maxwp + node, order_key(val));
+  if (dbits(val) != dbits(z)) atomicMax(wk.maxwp + node, order_key(val));
 }
 
 // PartWet1 level (src/MUSCLObject.cpp:86-112)
@@ -96,7 +116,7 @@ __device__ __forceinline__ double partwet1_level(const double* __restrict__ p, d
 }
 
 // ---------------------------------------------------------------- kernels
-template <bool BATCH>
+template <bool BATCH, bool COR0>
 __global__ void __launch_bounds__(256) k_recon1(DevMesh m, DevWork wk, const double* __restrict__ W,
                                                 const double* __restrict__ U, const double* __restrict__ V,
                                                 int latch_mode) {
@@ -127,7 +147,7 @@ __global__ void __launch_bounds__(256) k_recon1(DevMesh m, DevWork wk, const dou
       for (int k = 0; k < 3; ++k) {
         node_max(wk, m.cnode[k * C + i], dr[k], m.zn[k * C + i]);
         const int slot = k * C + i;
-        write_slot(wk, slot, m.ze[slot], dr[3 + k], 0., 0., dr[6], dr[7], cor);
+        write_slot<COR0>(wk, slot, m.ze[slot], dr[3 + k], 0., 0., dr[6], dr[7], cor);
       }
     } else if (!dlt(m.fwthr[i], w)) {
       // partially wet: PartWet1 now (node maxima), PartWet2 in k_recon2
@@ -203,8 +223,8 @@ __global__ void __launch_bounds__(256) k_recon1(DevMesh m, DevWork wk, const dou
         node_max(wk, m.cnode[slot], val, zk);
         const double be = m.ze[slot];
         double we;
-        if (at_point_wet(w, toff[k], be, &we)) write_slot(wk, slot, be, we, u, v, gx, gy, cor);
-        else write_slot(wk, slot, be, we, 0., 0., gx, gy, cor);
+        if (at_point_wet(w, toff[k], be, &we)) write_slot<COR0>(wk, slot, be, we, u, v, gx, gy, cor);
+        else write_slot<COR0>(wk, slot, be, we, 0., 0., gx, gy, cor);
       }
     }
   }
@@ -221,7 +241,7 @@ __global__ void __launch_bounds__(256) k_recon1(DevMesh m, DevWork wk, const dou
 }
 
 // ReconstructPartWetCell2 (src/MUSCLObject.cpp:114-191) over the listed cells.
-template <bool BATCH>
+template <bool BATCH, bool COR0>
 __global__ void __launch_bounds__(256) k_recon2(DevMesh m, DevWork wk, const double* __restrict__ W,
                                                 const double* __restrict__ U, const double* __restrict__ V) {
   const int C = m.C;
@@ -288,8 +308,8 @@ __global__ void __launch_bounds__(256) k_recon2(DevMesh m, DevWork wk, const dou
       const double be = m.ze[slot];
       const double off = plane ? (gx * r.dedge[k][0] + gy * r.dedge[k][1]) : 0.;
       double we;
-      if (at_point_wet(w0, off, be, &we)) write_slot(wk, slot, be, we, u, v, gx, gy, cor);
-      else write_slot(wk, slot, be, we, 0., 0., gx, gy, cor);
+      if (at_point_wet(w0, off, be, &we)) write_slot<COR0>(wk, slot, be, we, u, v, gx, gy, cor);
+      else write_slot<COR0>(wk, slot, be, we, 0., 0., gx, gy, cor);
     }
   }
 }
@@ -329,7 +349,7 @@ __global__ void __launch_bounds__(256) k_flux(DevMesh m, DevWork wk, const doubl
   // min-reduction of the length-to-wavespeed ratio on order-preserving integer
   // keys (exact): warp, block, one atomicMin per block and instance
   const unsigned long long kNone = ~0ull;
-  unsigned long long key = (__double_as_longlong(lw) == __double_as_longlong(kInf)) ? kNone : order_key(lw);
+  unsigned long long key = (dbits(lw) == dbits(kInf)) ? kNone : order_key(lw);
   const int lane = lane_id(), warp = threadIdx.x >> 5;
   const int inst0 = __shfl_sync(0xffffffffu, inst, 0);
   const bool warp_uniform = __all_sync(0xffffffffu, inst == inst0);
@@ -400,7 +420,9 @@ __global__ void __launch_bounds__(256) k_drain(DevMesh m, DevWork wk, const doub
 // reads its own cell before writing it, so no pointer here is __restrict__.
 // STORE_N also writes the state before ConsAssigner to nst [3][C] (for the
 // adjoint's segment recompute).
-template <bool BATCH, bool STORE_N = false>
+// HALF: a stage with a = b = c = 1/2 (SSPRK2's second), whose products with
+// the coefficients are exact halvings.
+template <bool BATCH, bool STORE_N, bool HALF>
 __global__ void __launch_bounds__(256) k_update(DevMesh m, DevWork wk, const double* Wp, const double* Up,
                                                 const double* Vp, const double* W0, const double* U0,
                                                 const double* V0, double* Wo, double* Uo, double* Vo, Stage st,
@@ -409,7 +431,7 @@ __global__ void __launch_bounds__(256) k_update(DevMesh m, DevWork wk, const dou
   if (i >= m.C) return;
   const int C = m.C;
   const int inst = BATCH ? m.cinst[i] : 0;
-  const double dt = st.first ? wk.dt[inst] : st.c * wk.dt[inst];
+  const double dt = HALF ? SWE_HALF(wk.dt[inst]) : (st.first ? wk.dt[inst] : st.c * wk.dt[inst]);
   const unsigned own = m.cown[i];
   const double dti = wk.drain[i];
   double r0 = 0., r1 = 0., r2 = 0.;
@@ -417,38 +439,45 @@ __global__ void __launch_bounds__(256) k_update(DevMesh m, DevWork wk, const dou
   for (int k = 0; k < 3; ++k) {
     const int slot = k * C + i;
     const int e = m.cedge[slot];
-    const double sgn = ((own >> k) & 1u) ? 1. : -1.;
+    // sgn = +1 for the edge's owner, else -1: products with it are sign changes
+    const bool out = (own >> k) & 1u;
     const double F0 = wk.f0[e], F1 = wk.f1[e], F2 = wk.f2[e];
     const int nb = m.cnbr[slot];
     const double dtik = nb < 0 ? kInf : wk.drain[nb];
-    const double dtk = dgt0(sgn * F0) ? smin(dt, dti) : smin(dt, dtik);
+    const double dtk = (out ? dgt0(F0) : dlt(F0, 0.)) ? smin(dt, dti) : smin(dt, dtik);  // sgn F0 > 0
     const double c_ek = m.cek[slot];
     const double h_ek = wk.ew[slot] - m.ze[slot];
-    const double s = dtk * sgn * c_ek;
+    const double s = (out ? dtk : SWE_NEG(dtk)) * c_ek;
     r0 -= s * F0;
     r1 -= s * F1;
     r2 -= s * F2;
     const double q = dt * (1. / 3.);
     r1 -= q * wk.sx[slot] * h_ek;
     r2 -= q * wk.sy[slot] * h_ek;
-    const double p = 0.5 * h_ek * h_ek;
-    r1 += dtk * (m.cnx[slot] * c_ek * p);
-    r2 += dtk * (m.cny[slot] * c_ek * p);
+    const double p = SWE_HALF(h_ek) * h_ek;  // 0.5 h h
+    r1 += dtk * (m.cnxc[slot] * p);        // (n_x c) p
+    r2 += dtk * (m.cnyc[slot] * p);
   }
   const double b = m.bc[i];
   const double h0 = W0[i] - b;
   const double c00 = h0, c01 = h0 * U0[i], c02 = h0 * V0[i];
   double n0, n1, n2;
-  if (st.first) {
+  if (st.first && !HALF) {
     n0 = c00 + r0;
     n1 = c01 + r1;
     n2 = c02 + r2;
   } else {
     const double hp = Wp[i] - b;
     const double c10 = hp, c11 = hp * Up[i], c12 = hp * Vp[i];
-    n0 = st.a * c00 + st.b * c10 + r0;
-    n1 = st.a * c01 + st.b * c11 + r1;
-    n2 = st.a * c02 + st.b * c12 + r2;
+    if (HALF) {
+      n0 = SWE_HALF(c00) + SWE_HALF(c10) + r0;
+      n1 = SWE_HALF(c01) + SWE_HALF(c11) + r1;
+      n2 = SWE_HALF(c02) + SWE_HALF(c12) + r2;
+    } else {
+      n0 = st.a * c00 + st.b * c10 + r0;
+      n1 = st.a * c01 + st.b * c11 + r1;
+      n2 = st.a * c02 + st.b * c12 + r2;
+    }
   }
   if (STORE_N) {
     nst[i] = n0;
@@ -460,7 +489,12 @@ __global__ void __launch_bounds__(256) k_update(DevMesh m, DevWork wk, const dou
   Wo[i] = ow;
   Uo[i] = ou;
   Vo[i] = ov;
-  if (!(isfinite(ow) && isfinite(ou) && isfinite(ov))) atomicOr(wk.err, kErrNonFinite);
+  // non-finite check on the exponent bits (integer pipe)
+  const unsigned long long xw = (unsigned long long)dbits(ow) >> 52,
+                           xu = (unsigned long long)dbits(ou) >> 52,
+                           xv = (unsigned long long)dbits(ov) >> 52;
+  if (((xw & 0x7FFull) == 0x7FFull) || ((xu & 0x7FFull) == 0x7FFull) || ((xv & 0x7FFull) == 0x7FFull))
+    atomicOr(wk.err, kErrNonFinite);
 }
 
 __global__ void k_init_nodes(DevMesh m, DevWork wk) {
@@ -521,6 +555,8 @@ std::string Engine::init(std::vector<HostInstance>&& inst, int flux, int ws, int
   cell_off[I] = C;
   edge_off[I] = E;
   node_off[I] = N;
+  cor0_ = true;
+  for (const auto& q : inst) cor0_ = cor0_ && q.cor == 0.;
   if (3 * C > (1ll << 31) - 1 || E > (1ll << 31) - 1 || N > (1ll << 31) - 1) {
     *st = 1;
     return "total mesh too large for int32 device indexing";
@@ -542,12 +578,12 @@ std::string Engine::init(std::vector<HostInstance>&& inst, int flux, int ws, int
   bool ok = true;
   const int *p_cnode, *p_cnbr, *p_cedge, *p_cinst, *p_eown, *p_enb, *p_esl, *p_esr, *p_einst, *p_icb;
   const unsigned char* p_cown;
-  const double *p_bc, *p_fw, *p_area, *p_zn, *p_ze, *p_cek, *p_cnx, *p_cny, *p_dry, *p_combo, *p_pw1, *p_enx, *p_eny,
+  const double *p_bc, *p_fw, *p_area, *p_zn, *p_ze, *p_cek, *p_cnxc, *p_cnyc, *p_dry, *p_combo, *p_pw1, *p_enx, *p_eny,
       *p_etx, *p_ety, *p_ezm, *p_elmin, *p_nz, *p_cfl, *p_cor;
   const Pw2Rec* p_pw2;
   ok = ok && up(img.cnode, p_cnode) && up(img.cnbr, p_cnbr) && up(img.cedge, p_cedge) && up(img.cinst, p_cinst);
   ok = ok && up(img.cown, p_cown) && up(img.bc, p_bc) && up(img.fwthr, p_fw) && up(img.area, p_area);
-  ok = ok && up(img.zn, p_zn) && up(img.ze, p_ze) && up(img.cek, p_cek) && up(img.cnx, p_cnx) && up(img.cny, p_cny);
+  ok = ok && up(img.zn, p_zn) && up(img.ze, p_ze) && up(img.cek, p_cek) && up(img.cnxc, p_cnxc) && up(img.cnyc, p_cnyc);
   ok = ok && up(img.dry, p_dry) && up(img.combo, p_combo) && up(img.pw1, p_pw1) && up(img.pw2, p_pw2);
   ok = ok && up(img.eown, p_eown) && up(img.enb, p_enb) && up(img.eslotl, p_esl) && up(img.eslotr, p_esr);
   ok = ok && up(img.einst, p_einst) && up(img.enx, p_enx) && up(img.eny, p_eny) && up(img.etx, p_etx);
@@ -559,7 +595,7 @@ std::string Engine::init(std::vector<HostInstance>&& inst, int flux, int ws, int
   }
   M.cnode = p_cnode; M.cnbr = p_cnbr; M.cedge = p_cedge; M.cinst = p_cinst; M.cown = p_cown;
   M.bc = p_bc; M.fwthr = p_fw; M.area = p_area; M.zn = p_zn; M.ze = p_ze; M.cek = p_cek;
-  M.cnx = p_cnx; M.cny = p_cny; M.dry = p_dry; M.combo = p_combo; M.pw1 = p_pw1; M.pw2 = p_pw2;
+  M.cnxc = p_cnxc; M.cnyc = p_cnyc; M.dry = p_dry; M.combo = p_combo; M.pw1 = p_pw1; M.pw2 = p_pw2;
   M.eown = p_eown; M.enb = p_enb; M.eslotl = p_esl; M.eslotr = p_esr; M.einst = p_einst;
   M.enx = p_enx; M.eny = p_eny; M.etx = p_etx; M.ety = p_ety; M.ezm = p_ezm; M.elmin = p_elmin;
   M.nz = p_nz; M.inst_cell_begin = p_icb; M.inst_cfl = p_cfl; M.inst_cor = p_cor;
@@ -628,14 +664,34 @@ cudaError_t Engine::reset_pass() {
   return cudaGetLastError();
 }
 
+void Engine::launch_recon1(const double* W, const double* U, const double* V, int latch_mode) {
+  const int b = block_, g = nblocks(mesh_.C, b);
+  if (batched_) {
+    if (cor0_) k_recon1<true, true><<<g, b, 0, stream_>>>(mesh_, work_, W, U, V, latch_mode);
+    else k_recon1<true, false><<<g, b, 0, stream_>>>(mesh_, work_, W, U, V, latch_mode);
+  } else {
+    if (cor0_) k_recon1<false, true><<<g, b, 0, stream_>>>(mesh_, work_, W, U, V, latch_mode);
+    else k_recon1<false, false><<<g, b, 0, stream_>>>(mesh_, work_, W, U, V, latch_mode);
+  }
+  ++launches_;
+}
+
+void Engine::launch_recon2(const double* W, const double* U, const double* V) {
+  const int b = block_, g = std::max(1, std::min(nblocks(mesh_.C, b), 152 * 8));
+  if (batched_) {
+    if (cor0_) k_recon2<true, true><<<g, b, 0, stream_>>>(mesh_, work_, W, U, V);
+    else k_recon2<true, false><<<g, b, 0, stream_>>>(mesh_, work_, W, U, V);
+  } else {
+    if (cor0_) k_recon2<false, true><<<g, b, 0, stream_>>>(mesh_, work_, W, U, V);
+    else k_recon2<false, false><<<g, b, 0, stream_>>>(mesh_, work_, W, U, V);
+  }
+  ++launches_;
+}
+
 cudaError_t Engine::interface_values(const double* W, const double* U, const double* V, int latch_mode) {
   const int b = block_;
-  if (batched_) k_recon1<true><<<nblocks(mesh_.C, b), b, 0, stream_>>>(mesh_, work_, W, U, V, latch_mode);
-  else k_recon1<false><<<nblocks(mesh_.C, b), b, 0, stream_>>>(mesh_, work_, W, U, V, latch_mode);
-  const int g2 = std::max(1, std::min(nblocks(mesh_.C, b), 152 * 8));
-  if (batched_) k_recon2<true><<<g2, b, 0, stream_>>>(mesh_, work_, W, U, V);
-  else k_recon2<false><<<g2, b, 0, stream_>>>(mesh_, work_, W, U, V);
-  launches_ += 2;
+  launch_recon1(W, U, V, latch_mode);
+  launch_recon2(W, U, V);
   return cudaGetLastError();
 }
 
@@ -665,28 +721,44 @@ cudaError_t Engine::launch_stage(const Stage& st, const double* const* in, const
   const int b = block_;
   const int lm = first_stage_of_step ? latch_mode : 0;
   if (ev) cudaEventRecord(ev[0], stream_);
-  if (batched_) k_recon1<true><<<nblocks(mesh_.C, b), b, 0, stream_>>>(mesh_, work_, in[0], in[1], in[2], lm);
-  else k_recon1<false><<<nblocks(mesh_.C, b), b, 0, stream_>>>(mesh_, work_, in[0], in[1], in[2], lm);
+  launch_recon1(in[0], in[1], in[2], lm);
   if (ev) cudaEventRecord(ev[1], stream_);
-  const int g2 = std::max(1, std::min(nblocks(mesh_.C, b), 152 * 8));
-  if (batched_) k_recon2<true><<<g2, b, 0, stream_>>>(mesh_, work_, in[0], in[1], in[2]);
-  else k_recon2<false><<<g2, b, 0, stream_>>>(mesh_, work_, in[0], in[1], in[2]);
-  launches_ += 2;
+  launch_recon2(in[0], in[1], in[2]);
   if (ev) cudaEventRecord(ev[2], stream_);
   cudaError_t e = fluxes(in[0]);
   if (e != cudaSuccess) return e;
   if (ev) cudaEventRecord(ev[3], stream_);
   k_drain<<<nblocks(std::max(mesh_.C, mesh_.N), b), b, 0, stream_>>>(mesh_, work_, in[0]);
   if (ev) cudaEventRecord(ev[4], stream_);
-  if (batched_)
-    k_update<true><<<nblocks(mesh_.C, b), b, 0, stream_>>>(mesh_, work_, in[0], in[1], in[2], u0[0], u0[1], u0[2],
-                                                           out[0], out[1], out[2], st);
-  else
-    k_update<false><<<nblocks(mesh_.C, b), b, 0, stream_>>>(mesh_, work_, in[0], in[1], in[2], u0[0], u0[1],
-                                                            u0[2], out[0], out[1], out[2], st);
+  ++launches_;
+  launch_update(st, in, u0, out, nullptr);
   if (ev) cudaEventRecord(ev[5], stream_);
-  launches_ += 2;
   return cudaGetLastError();
+}
+
+template <bool BATCH, bool STORE_N, bool HALF>
+static void update_kernel(int g, int b, cudaStream_t s, const DevMesh& m, const DevWork& w, const Stage& st,
+                          const double* const* in, const double* const* u0, double* const* out, double* nst) {
+  k_update<BATCH, STORE_N, HALF><<<g, b, 0, s>>>(m, w, in[0], in[1], in[2], u0[0], u0[1], u0[2], out[0], out[1],
+                                                 out[2], st, nst);
+}
+
+void Engine::launch_update(const Stage& st, const double* const* in, const double* const* u0, double* const* out,
+                           double* nst) {
+  const int b = block_, g = nblocks(mesh_.C, b);
+  const bool half = !st.first && st.a == 0.5 && st.b == 0.5 && st.c == 0.5;
+  const int sel = (batched_ ? 4 : 0) | (nst ? 2 : 0) | (half ? 1 : 0);
+  switch (sel) {
+    case 0: update_kernel<false, false, false>(g, b, stream_, mesh_, work_, st, in, u0, out, nst); break;
+    case 1: update_kernel<false, false, true>(g, b, stream_, mesh_, work_, st, in, u0, out, nst); break;
+    case 2: update_kernel<false, true, false>(g, b, stream_, mesh_, work_, st, in, u0, out, nst); break;
+    case 3: update_kernel<false, true, true>(g, b, stream_, mesh_, work_, st, in, u0, out, nst); break;
+    case 4: update_kernel<true, false, false>(g, b, stream_, mesh_, work_, st, in, u0, out, nst); break;
+    case 5: update_kernel<true, false, true>(g, b, stream_, mesh_, work_, st, in, u0, out, nst); break;
+    case 6: update_kernel<true, true, false>(g, b, stream_, mesh_, work_, st, in, u0, out, nst); break;
+    default: update_kernel<true, true, true>(g, b, stream_, mesh_, work_, st, in, u0, out, nst); break;
+  }
+  ++launches_;
 }
 
 cudaError_t Engine::step_timed(int scheme, int latch_mode, double* acc) {
@@ -722,14 +794,7 @@ cudaError_t Engine::step_timed(int scheme, int latch_mode, double* acc) {
 
 cudaError_t Engine::update_only(const Stage& st, const double* const* in, const double* const* u0,
                                 double* const* out, double* nst) {
-  const int b = block_;
-  if (batched_)
-    k_update<true, true><<<nblocks(mesh_.C, b), b, 0, stream_>>>(mesh_, work_, in[0], in[1], in[2], u0[0], u0[1],
-                                                                 u0[2], out[0], out[1], out[2], st, nst);
-  else
-    k_update<false, true><<<nblocks(mesh_.C, b), b, 0, stream_>>>(mesh_, work_, in[0], in[1], in[2], u0[0], u0[1],
-                                                                  u0[2], out[0], out[1], out[2], st, nst);
-  ++launches_;
+  launch_update(st, in, u0, out, nst);
   return cudaGetLastError();
 }
 

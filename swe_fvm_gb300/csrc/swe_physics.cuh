@@ -29,6 +29,14 @@ namespace swe {
 #define SWE_DIV(a, b) ((a) / (b))
 #define SWE_SQRT(x) std::sqrt((x))
 #endif
+// 0.5 x and -x (exact operations; on the device without FP64 instructions)
+#if defined(__CUDA_ARCH__)
+#define SWE_HALF(x) ::swe::dhalf_rn((x))
+#define SWE_NEG(x) ::swe::dneg((x))
+#else
+#define SWE_HALF(x) (0.5 * (x))
+#define SWE_NEG(x) (-(x))
+#endif
 
 // include/Includes.h:30
 constexpr double kTol = 1e-13;
@@ -52,10 +60,10 @@ constexpr double kSqrt2 = 1.4142135623730951;  // std::sqrt(2), correctly rounde
 // host keeps the IEEE comparisons: the two agree on every non-NaN input.
 #if defined(__CUDA_ARCH__)
 __device__ __forceinline__ long long fkey(double x) {
-  const long long i = __double_as_longlong(x);
+  const long long i = dbits(x);
   return i < 0 ? -(i & 0x7FFFFFFFFFFFFFFFll) : i;
 }
-__device__ __forceinline__ long long fbits(double x) { return __double_as_longlong(x); }
+__device__ __forceinline__ long long fbits(double x) { return dbits(x); }
 SWE_HD bool dlt(double a, double b) { return fkey(a) < fkey(b); }
 SWE_HD bool dle(double a, double b) { return fkey(a) <= fkey(b); }
 // x > c and x < c for a constant c > 0: the signed bit patterns order them
@@ -190,7 +198,7 @@ SWE_HD double bisection(double d, double c, double b, double xmin, double xmax) 
   double x = 0.;
   bool smin_ = signbit(fmin_);
   for (int it = 0; it <= n; it++) {
-    x = 0.5 * (xmin + xmax);
+    x = SWE_HALF(xmin + xmax);
     double fx = cubic(d, c, b, x);
     bool sx = signbit(fx);
     if (smin_ != sx) {
@@ -241,8 +249,9 @@ SWE_HD void elem_flux(double nx, double ny, double h, double hu, double hv, doub
     double hveln = hu * nx + hv * ny;
     f[0] = hveln;
     const double q = SWE_DIV(hveln, h);
-    f[1] = q * hu + (0.5 * h * h) * nx;
-    f[2] = q * hv + (0.5 * h * h) * ny;
+    const double p = SWE_HALF(h) * h;  // 0.5 h h
+    f[1] = q * hu + p * nx;
+    f[2] = q * hv + p * ny;
   }
 }
 
@@ -270,7 +279,7 @@ struct Einfeldt {
   SWE_HD static void speeds(double ul, double hl, double ur, double hr, double* a0, double* a1) {
     double cl = SWE_SQRT(hl), cr = SWE_SQRT(hr);
     double uRoe = SWE_DIV(cl * ul + cl * ur, cl + cr);  // the reference's cl * ur
-    double cRoe = SWE_SQRT(0.5 * (hl + hr));
+    double cRoe = SWE_SQRT(SWE_HALF(hl + hr));
     *a0 = smin(ul - cl, uRoe - cRoe);
     *a1 = smax(ur + cr, uRoe + cRoe);
   }
@@ -325,47 +334,48 @@ struct HLLC {
   SWE_HD static void eval(const EdgeGeom& g, const SideState& L, const SideState& R, double cor, double* lw,
                           double* F) {
     double ul = L.u * g.nx + L.v * g.ny;
-    double vl = L.u * g.tx + L.v * g.ty;
     double hl = L.w - g.b;
     double ur = R.u * g.nx + R.v * g.ny;
-    double vr = R.u * g.tx + R.v * g.ty;
     double hr = R.w - g.b;
     F[0] = 0.; F[1] = 0.; F[2] = 0.;
     if (!dgtc(hl + hr, kMinCapture)) return;
     double al, ar;
     W::speeds(ul, hl, ur, hr, &al, &ar);
-    double ustar = (ar - ur) * hr * ur - (al - ul) * hl * ul + 0.5 * (hl * hl - hr * hr);
+    double ustar = (ar - ur) * hr * ur - (al - ul) * hl * ul + SWE_HALF(hl * hl - hr * hr);
     ustar = SWE_DIV(ustar, hr * (ar - ur) - hl * (al - ul));
     *lw = SWE_DIV(g.lmin, fabs(cor) + smax(kTol, smax(al, ar)));
-    if (!dgt0(ustar)) {
-      double Ur[3] = {hr, hr * R.u, hr * R.v};
-      double us = vr * g.tx + ustar * g.ty;
-      double vs = vr * g.nx + ustar * g.ny;
-      double hs = SWE_DIV(hr * (ar - ur), ar - ustar);
-      double Us[3] = {hs, hs * us, hs * vs};
-      double Fr[3];
-      elem_flux(g.nx, g.ny, Ur[0], Ur[1], Ur[2], Fr);
-      double s = smax(0., ar);
+    // u* <= 0: the right star state, else the left one.  The side is picked
+    // first and the shared formula evaluated once, so a warp whose edges take
+    // both sides issues it once (the operations per side are the reference's).
+    const bool right = !dgt0(ustar);
+    const double hx = right ? hr : hl, ux = right ? R.u : L.u, vx = right ? R.v : L.v;
+    const double ax = right ? ar : al, unx = right ? ur : ul;
+    const double vt = ux * g.tx + vx * g.ty;  // tangential velocity of that side
+    double Ux[3] = {hx, hx * ux, hx * vx};
+    double us = vt * g.tx + ustar * g.ty;
+    double vs = vt * g.nx + ustar * g.ny;
+    double hs = SWE_DIV(hx * (ax - unx), ax - ustar);
+    double Us[3] = {hs, hs * us, hs * vs};
+    double Fx[3];
+    elem_flux(g.nx, g.ny, Ux[0], Ux[1], Ux[2], Fx);
+    double s = right ? smax(0., ar) : smin(0., al);
 #pragma unroll
-      for (int q = 0; q < 3; ++q) F[q] = Fr[q] + s * (Us[q] - Ur[q]);
-    } else {
-      double Ul[3] = {hl, hl * L.u, hl * L.v};
-      double us = vl * g.tx + ustar * g.ty;
-      double vs = vl * g.nx + ustar * g.ny;
-      double hs = SWE_DIV(hl * (al - ul), al - ustar);
-      double Us[3] = {hs, hs * us, hs * vs};
-      double Fl[3];
-      elem_flux(g.nx, g.ny, Ul[0], Ul[1], Ul[2], Fl);
-      double s = smin(0., al);
-#pragma unroll
-      for (int q = 0; q < 3; ++q) F[q] = Fl[q] + s * (Us[q] - Ul[q]);
-    }
+    for (int q = 0; q < 3; ++q) F[q] = Fx[q] + s * (Us[q] - Ux[q]);
   }
 };
 
 // ------------------------------------------------------- ordered doubles
 // Monotone map of doubles to unsigned 64-bit keys (for non-NaN values), so
 // that integer atomicMax / atomicMin give the exact floating-point max / min.
+#if defined(__CUDA_ARCH__)
+__device__ __forceinline__ unsigned long long order_key(double d) {
+  const unsigned long long u = (unsigned long long)dbits(d);
+  return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double order_val(unsigned long long k) {
+  return dfrom((long long)((k >> 63) ? (k & 0x7FFFFFFFFFFFFFFFull) : ~k));
+}
+#else
 SWE_HD unsigned long long order_key(double d) {
   union {
     double d;
@@ -382,5 +392,6 @@ SWE_HD double order_val(unsigned long long k) {
   c.u = (k >> 63) ? (k & 0x7FFFFFFFFFFFFFFFull) : ~k;
   return c.d;
 }
+#endif
 
 }  // namespace swe

@@ -24,7 +24,7 @@ void HostImage::resize(int C_, int E_, int N_, int I_) {
   cinst.assign(C, 0); cown.assign(C, 0);
   bc.assign(C, 0); fwthr.assign(C, 0); area.assign(C, 0);
   zn.assign(3 * (size_t)C, 0); ze.assign(3 * (size_t)C, 0); cek.assign(3 * (size_t)C, 0);
-  cnx.assign(3 * (size_t)C, 0); cny.assign(3 * (size_t)C, 0);
+  cnxc.assign(3 * (size_t)C, 0); cnyc.assign(3 * (size_t)C, 0);
   dry.assign((size_t)C * kDryStride, 0); combo.assign((size_t)C * 8 * kComboStride, 0);
   pw1.assign((size_t)C * kPw1Stride, 0); pw2.assign(C, Pw2Rec{});
   eown.assign(E, 0); enb.assign(E, -1); eslotl.assign(E, 0); eslotr.assign(E, -1); einst.assign(E, 0);
@@ -182,8 +182,10 @@ void precompute_instance(const HostInstance& h, int inst, int64_t c0, int64_t e0
         img.cek[k * Ct + gi] = i_area * g.L(ie[k]);  // src/TimeDisc.cpp:17,28
         double nrm[2];
         g.Norm(ie[k], i, nrm);  // src/TimeDisc.cpp:35
-        img.cnx[k * Ct + gi] = nrm[0];
-        img.cny[k * Ct + gi] = nrm[1];
+        // n c: the pressure term's geometry factor (src/TimeDisc.cpp:35 evaluates
+        // n(e, i) * c first), kept whole so the update multiplies once
+        img.cnxc[k * Ct + gi] = nrm[0] * img.cek[k * Ct + gi];
+        img.cnyc[k * Ct + gi] = nrm[1] * img.cek[k * Ct + gi];
       }
       // ---- dry cell: ReconstructDryCell + UpdateInterfaceValues
       // (src/MUSCLObject.cpp:31-36, include/MUSCLObject.h:26-33, src/Assigners.cpp:8-20)
