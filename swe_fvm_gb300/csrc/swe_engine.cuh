@@ -96,6 +96,7 @@ struct DevWork {
   int* pwlist;                 // [C] partially-wet cells of this stage
   int* pwcount;                // [1]
   double* pwrec;               // [C] PartWet1 level of listed cells
+  unsigned char* pwflag;       // [C] 1 for the stage's partially-wet cells (pass 1)
   unsigned long long* r;       // [I] ordered key of min length-to-wavespeed
   double* dt;                  // [I] step dt
   double* tsum;                // [I] accumulated time
@@ -211,11 +212,19 @@ class Engine {
   std::vector<void*> allocs_;
   cudaStream_t stream_ = nullptr;
   cudaStream_t own_stream_ = nullptr;
+  // second stream of a stage: PartWet2 and the fluxes of the edges next to
+  // partially-wet cells run on it while the other edges' fluxes run on stream_
+  cudaStream_t side_ = nullptr;
+  cudaEvent_t ev_fork_ = nullptr, ev_join_ = nullptr;
   int flux_ = 1, ws_ = 2, block_ = 256;
   bool batched_ = false;
   bool cor0_ = true;  // every instance has cor = 0: no Coriolis arithmetic in the reconstruction
   void launch_recon1(const double* W, const double* U, const double* V, int latch_mode);
-  void launch_recon2(const double* W, const double* U, const double* V);
+  void launch_recon2(const double* W, const double* U, const double* V, cudaStream_t s);
+  // fluxes: mode 0 every edge; mode 1 the edges with no partially-wet cell;
+  // fluxes_pw: the others (those of the listed cells), on stream s
+  cudaError_t fluxes(const double* W, int mode);
+  void fluxes_pw(const double* W, cudaStream_t s);
   void launch_update(const Stage& st, const double* const* in, const double* const* u0, double* const* out,
                      double* nst);
   int64_t launches_ = 0;

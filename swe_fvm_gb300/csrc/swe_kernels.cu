@@ -228,6 +228,7 @@ __global__ void __launch_bounds__(256) k_recon1(DevMesh m, DevWork wk, const dou
       }
     }
   }
+  if (i < m.C) wk.pwflag[i] = part ? 1 : 0;
   // warp-aggregated append of the partially-wet cells
   const unsigned bal = __ballot_sync(0xffffffffu, part);
   if (bal) {
@@ -315,7 +316,37 @@ __global__ void __launch_bounds__(256) k_recon2(DevMesh m, DevWork wk, const dou
 }
 
 // SpaceDisc::ComputeFluxes with flux plugin FLUX and the CFL min-reduction.
-template <class FLUX, bool BATCH>
+// The flux of edge e (src/SpaceDisc.cpp:54-74) into f0..f2; *lw receives its
+// length-to-wavespeed ratio or stays +inf.
+template <class FLUX>
+__device__ __forceinline__ void flux_edge(const DevMesh& m, const DevWork& wk, const double* __restrict__ W, int e,
+                                          int inst, double* lw) {
+  const int o = m.eown[e];
+  const int nb = m.enb[e];
+  double F[3];
+  const double nx = m.enx[e], ny = m.eny[e];
+  if (nb < 0) {
+    // solid wall: ElemFlux with the owner's cell-average depth (src/SpaceDisc.cpp:66-69)
+    elem_flux(nx, ny, W[o] - m.bc[o], 0., 0., F);
+  } else {
+    EdgeGeom g;
+    g.nx = nx; g.ny = ny;
+    g.tx = m.etx[e]; g.ty = m.ety[e];
+    g.b = m.ezm[e];
+    g.lmin = m.elmin[e];
+    const int sl = m.eslotl[e], sr = m.eslotr[e];
+    SideState L{wk.ew[sl], wk.eu[sl], wk.ev[sl]};
+    SideState R{wk.ew[sr], wk.eu[sr], wk.ev[sr]};
+    FLUX::eval(g, L, R, m.inst_cor[inst], lw, F);
+  }
+  wk.f0[e] = F[0];
+  wk.f1[e] = F[1];
+  wk.f2[e] = F[2];
+}
+
+// MODE 0: every edge.  MODE 1: the edges none of whose cells is partially
+// wet (the others wait for PartWet2 and go through k_flux_pw).
+template <class FLUX, bool BATCH, int MODE>
 __global__ void __launch_bounds__(256) k_flux(DevMesh m, DevWork wk, const double* __restrict__ W) {
   __shared__ unsigned long long s_min[32];
   __shared__ int s_inst[32];
@@ -324,27 +355,12 @@ __global__ void __launch_bounds__(256) k_flux(DevMesh m, DevWork wk, const doubl
   int inst = 0;
   if (e < m.E) {
     if (BATCH) inst = m.einst[e];
-    const int o = m.eown[e];
-    const int nb = m.enb[e];
-    double F[3];
-    const double nx = m.enx[e], ny = m.eny[e];
-    if (nb < 0) {
-      // solid wall: ElemFlux with the owner's cell-average depth (src/SpaceDisc.cpp:66-69)
-      elem_flux(nx, ny, W[o] - m.bc[o], 0., 0., F);
-    } else {
-      EdgeGeom g;
-      g.nx = nx; g.ny = ny;
-      g.tx = m.etx[e]; g.ty = m.ety[e];
-      g.b = m.ezm[e];
-      g.lmin = m.elmin[e];
-      const int sl = m.eslotl[e], sr = m.eslotr[e];
-      SideState L{wk.ew[sl], wk.eu[sl], wk.ev[sl]};
-      SideState R{wk.ew[sr], wk.eu[sr], wk.ev[sr]};
-      FLUX::eval(g, L, R, m.inst_cor[inst], &lw, F);
+    bool mine = true;
+    if (MODE == 1) {
+      const int nb = m.enb[e];
+      mine = !(wk.pwflag[m.eown[e]] | (nb >= 0 ? wk.pwflag[nb] : (unsigned char)0));
     }
-    wk.f0[e] = F[0];
-    wk.f1[e] = F[1];
-    wk.f2[e] = F[2];
+    if (mine) flux_edge<FLUX>(m, wk, W, e, inst, &lw);
   }
   // min-reduction of the length-to-wavespeed ratio on order-preserving integer
   // keys (exact): warp, block, one atomicMin per block and instance
@@ -387,6 +403,26 @@ __global__ void __launch_bounds__(256) k_flux(DevMesh m, DevWork wk, const doubl
     } else if (v != kNone && vi >= 0) {
       atomicMin(wk.r + vi, v);
     }
+  }
+}
+
+// The fluxes of the edges next to the stage's partially-wet cells (after
+// PartWet2): listed cell i takes its local edge k unless the edge's owner is
+// partially wet too and is not i, so that each edge is evaluated once.
+template <class FLUX, bool BATCH>
+__global__ void __launch_bounds__(128) k_flux_pw(DevMesh m, DevWork wk, const double* __restrict__ W) {
+  const int C = m.C;
+  const int n = 3 * min(*wk.pwcount, C);
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    const int q = t / 3, k = t - 3 * q;
+    const int i = wk.pwlist[q];
+    const int e = m.cedge[k * C + i];
+    const int o = m.eown[e];
+    if ((wk.pwflag[o] ? o : m.enb[e]) != i) continue;
+    const int inst = BATCH ? m.einst[e] : 0;
+    double lw = kInf;
+    flux_edge<FLUX>(m, wk, W, e, inst, &lw);
+    if (dbits(lw) != dbits(kInf)) atomicMin(wk.r + inst, order_key(lw));
   }
 }
 
@@ -525,6 +561,9 @@ Engine::~Engine() {
   for (void* p : allocs_) cudaFree(p);
   if (h_fixed_dt) cudaFreeHost(h_fixed_dt);
   if (own_stream_) cudaStreamDestroy(own_stream_);
+  if (side_) cudaStreamDestroy(side_);
+  if (ev_fork_) cudaEventDestroy(ev_fork_);
+  if (ev_join_) cudaEventDestroy(ev_join_);
 }
 
 std::string Engine::init(std::vector<HostInstance>&& inst, int flux, int ws, int block, int* st, bool batched) {
@@ -609,6 +648,7 @@ std::string Engine::init(std::vector<HostInstance>&& inst, int flux, int ws, int
   Wk.pwlist = dalloc<int>(C);
   Wk.pwcount = dalloc<int>(1);
   Wk.pwrec = dalloc<double>(C);
+  Wk.pwflag = dalloc<unsigned char>(C);
   Wk.r = dalloc<unsigned long long>(I);
   Wk.dt = dalloc<double>(I);
   Wk.tsum = dalloc<double>(I);
@@ -619,7 +659,7 @@ std::string Engine::init(std::vector<HostInstance>&& inst, int flux, int ws, int
   d_io = dalloc<double>(3 * C);
   d_ioflag = dalloc<unsigned>(1);
   if (!Wk.ew || !Wk.eu || !Wk.ev || !Wk.sx || !Wk.sy || !Wk.f0 || !Wk.f1 || !Wk.f2 || !Wk.drain || !Wk.maxwp ||
-      !Wk.pwlist || !Wk.pwcount || !Wk.pwrec || !Wk.r || !Wk.dt || !Wk.tsum || !d_fixed_dt || !Wk.err ||
+      !Wk.pwlist || !Wk.pwcount || !Wk.pwrec || !Wk.pwflag || !Wk.r || !Wk.dt || !Wk.tsum || !d_fixed_dt || !Wk.err ||
       !state_[5] || !d_io || !d_ioflag) {
     *st = 6;
     return "device allocation failed";
@@ -642,7 +682,10 @@ std::string Engine::init(std::vector<HostInstance>&& inst, int flux, int ws, int
   cudaMemset(Wk.err, 0, sizeof(unsigned));
   std::vector<unsigned long long> one(I, order_key(1.0));
   cudaMemcpy(Wk.r, one.data(), I * sizeof(unsigned long long), cudaMemcpyHostToDevice);
-  if (cudaStreamCreateWithFlags(&own_stream_, cudaStreamNonBlocking) != cudaSuccess) {
+  if (cudaStreamCreateWithFlags(&own_stream_, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&side_, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&ev_fork_, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&ev_join_, cudaEventDisableTiming) != cudaSuccess) {
     *st = 5;
     return "stream creation failed";
   }
@@ -676,14 +719,14 @@ void Engine::launch_recon1(const double* W, const double* U, const double* V, in
   ++launches_;
 }
 
-void Engine::launch_recon2(const double* W, const double* U, const double* V) {
+void Engine::launch_recon2(const double* W, const double* U, const double* V, cudaStream_t s) {
   const int b = block_, g = std::max(1, std::min(nblocks(mesh_.C, b), 152 * 8));
   if (batched_) {
-    if (cor0_) k_recon2<true, true><<<g, b, 0, stream_>>>(mesh_, work_, W, U, V);
-    else k_recon2<true, false><<<g, b, 0, stream_>>>(mesh_, work_, W, U, V);
+    if (cor0_) k_recon2<true, true><<<g, b, 0, s>>>(mesh_, work_, W, U, V);
+    else k_recon2<true, false><<<g, b, 0, s>>>(mesh_, work_, W, U, V);
   } else {
-    if (cor0_) k_recon2<false, true><<<g, b, 0, stream_>>>(mesh_, work_, W, U, V);
-    else k_recon2<false, false><<<g, b, 0, stream_>>>(mesh_, work_, W, U, V);
+    if (cor0_) k_recon2<false, true><<<g, b, 0, s>>>(mesh_, work_, W, U, V);
+    else k_recon2<false, false><<<g, b, 0, s>>>(mesh_, work_, W, U, V);
   }
   ++launches_;
 }
@@ -691,29 +734,55 @@ void Engine::launch_recon2(const double* W, const double* U, const double* V) {
 cudaError_t Engine::interface_values(const double* W, const double* U, const double* V, int latch_mode) {
   const int b = block_;
   launch_recon1(W, U, V, latch_mode);
-  launch_recon2(W, U, V);
+  launch_recon2(W, U, V, stream_);
   return cudaGetLastError();
 }
 
 template <class FLUX>
-static void launch_flux(bool batched, int blocks, int b, cudaStream_t s, const DevMesh& m, const DevWork& w,
-                        const double* W) {
-  if (batched) k_flux<FLUX, true><<<blocks, b, 0, s>>>(m, w, W);
-  else k_flux<FLUX, false><<<blocks, b, 0, s>>>(m, w, W);
+static void launch_flux(bool batched, int mode, int blocks, int b, cudaStream_t s, const DevMesh& m,
+                        const DevWork& w, const double* W) {
+  if (batched) {
+    if (mode) k_flux<FLUX, true, 1><<<blocks, b, 0, s>>>(m, w, W);
+    else k_flux<FLUX, true, 0><<<blocks, b, 0, s>>>(m, w, W);
+  } else {
+    if (mode) k_flux<FLUX, false, 1><<<blocks, b, 0, s>>>(m, w, W);
+    else k_flux<FLUX, false, 0><<<blocks, b, 0, s>>>(m, w, W);
+  }
+}
+template <class FLUX>
+static void launch_flux_pw(bool batched, int blocks, cudaStream_t s, const DevMesh& m, const DevWork& w,
+                           const double* W) {
+  if (batched) k_flux_pw<FLUX, true><<<blocks, 128, 0, s>>>(m, w, W);
+  else k_flux_pw<FLUX, false><<<blocks, 128, 0, s>>>(m, w, W);
 }
 
-cudaError_t Engine::fluxes(const double* W) {
+cudaError_t Engine::fluxes(const double* W) { return fluxes(W, 0); }
+
+cudaError_t Engine::fluxes(const double* W, int mode) {
   const int b = block_, g = nblocks(mesh_.E, b);
   switch (flux_ * 3 + ws_) {
-    case 0: launch_flux<HLL<Rusanov>>(batched_, g, b, stream_, mesh_, work_, W); break;
-    case 1: launch_flux<HLL<Davis>>(batched_, g, b, stream_, mesh_, work_, W); break;
-    case 2: launch_flux<HLL<Einfeldt>>(batched_, g, b, stream_, mesh_, work_, W); break;
-    case 3: launch_flux<HLLC<Rusanov>>(batched_, g, b, stream_, mesh_, work_, W); break;
-    case 4: launch_flux<HLLC<Davis>>(batched_, g, b, stream_, mesh_, work_, W); break;
-    default: launch_flux<HLLC<Einfeldt>>(batched_, g, b, stream_, mesh_, work_, W); break;
+    case 0: launch_flux<HLL<Rusanov>>(batched_, mode, g, b, stream_, mesh_, work_, W); break;
+    case 1: launch_flux<HLL<Davis>>(batched_, mode, g, b, stream_, mesh_, work_, W); break;
+    case 2: launch_flux<HLL<Einfeldt>>(batched_, mode, g, b, stream_, mesh_, work_, W); break;
+    case 3: launch_flux<HLLC<Rusanov>>(batched_, mode, g, b, stream_, mesh_, work_, W); break;
+    case 4: launch_flux<HLLC<Davis>>(batched_, mode, g, b, stream_, mesh_, work_, W); break;
+    default: launch_flux<HLLC<Einfeldt>>(batched_, mode, g, b, stream_, mesh_, work_, W); break;
   }
   launches_ += 1;
   return cudaGetLastError();
+}
+
+void Engine::fluxes_pw(const double* W, cudaStream_t s) {
+  const int g = std::max(1, std::min((3 * (int)mesh_.C + 127) / 128, 152 * 8));
+  switch (flux_ * 3 + ws_) {
+    case 0: launch_flux_pw<HLL<Rusanov>>(batched_, g, s, mesh_, work_, W); break;
+    case 1: launch_flux_pw<HLL<Davis>>(batched_, g, s, mesh_, work_, W); break;
+    case 2: launch_flux_pw<HLL<Einfeldt>>(batched_, g, s, mesh_, work_, W); break;
+    case 3: launch_flux_pw<HLLC<Rusanov>>(batched_, g, s, mesh_, work_, W); break;
+    case 4: launch_flux_pw<HLLC<Davis>>(batched_, g, s, mesh_, work_, W); break;
+    default: launch_flux_pw<HLLC<Einfeldt>>(batched_, g, s, mesh_, work_, W); break;
+  }
+  launches_ += 1;
 }
 
 cudaError_t Engine::launch_stage(const Stage& st, const double* const* in, const double* const* u0,
@@ -722,12 +791,26 @@ cudaError_t Engine::launch_stage(const Stage& st, const double* const* in, const
   const int lm = first_stage_of_step ? latch_mode : 0;
   if (ev) cudaEventRecord(ev[0], stream_);
   launch_recon1(in[0], in[1], in[2], lm);
-  if (ev) cudaEventRecord(ev[1], stream_);
-  launch_recon2(in[0], in[1], in[2]);
-  if (ev) cudaEventRecord(ev[2], stream_);
-  cudaError_t e = fluxes(in[0]);
-  if (e != cudaSuccess) return e;
-  if (ev) cudaEventRecord(ev[3], stream_);
+  if (ev) {
+    // per-kernel timing: the kernels one after another
+    cudaEventRecord(ev[1], stream_);
+    launch_recon2(in[0], in[1], in[2], stream_);
+    cudaEventRecord(ev[2], stream_);
+    cudaError_t e = fluxes(in[0], 0);
+    if (e != cudaSuccess) return e;
+    cudaEventRecord(ev[3], stream_);
+  } else {
+    // PartWet2 and the fluxes next to partially-wet cells on the side stream,
+    // beside the other edges' fluxes
+    cudaEventRecord(ev_fork_, stream_);
+    cudaStreamWaitEvent(side_, ev_fork_, 0);
+    launch_recon2(in[0], in[1], in[2], side_);
+    fluxes_pw(in[0], side_);
+    cudaEventRecord(ev_join_, side_);
+    cudaError_t e = fluxes(in[0], 1);
+    if (e != cudaSuccess) return e;
+    cudaStreamWaitEvent(stream_, ev_join_, 0);
+  }
   k_drain<<<nblocks(std::max(mesh_.C, mesh_.N), b), b, 0, stream_>>>(mesh_, work_, in[0]);
   if (ev) cudaEventRecord(ev[4], stream_);
   ++launches_;
@@ -849,7 +932,7 @@ cudaError_t Engine::run_graph(int scheme, int latch_mode, int64_t n) {
     }
     launches_ = per_step;  // capture launched nothing
   }
-  const int64_t kernels_per_step = 5 * scheme_table(scheme).n;
+  const int64_t kernels_per_step = 6 * scheme_table(scheme).n;
   for (int64_t s = 0; s < n; ++s) {
     cudaError_t e = cudaGraphLaunch(ge, stream_);
     if (e != cudaSuccess) return e;

@@ -341,20 +341,23 @@ struct HLLC {
     if (!dgtc(hl + hr, kMinCapture)) return;
     double al, ar;
     W::speeds(ul, hl, ur, hr, &al, &ar);
-    double ustar = (ar - ur) * hr * ur - (al - ul) * hl * ul + SWE_HALF(hl * hl - hr * hr);
-    ustar = SWE_DIV(ustar, hr * (ar - ur) - hl * (al - ul));
+    // (ar - ur) hr = hr (ar - ur) and (al - ul) hl = hl (al - ul) bit for bit:
+    // each product is formed once for u* and the star depth
+    const double hrA = (ar - ur) * hr, hlB = (al - ul) * hl;
+    double ustar = hrA * ur - hlB * ul + SWE_HALF(hl * hl - hr * hr);
+    ustar = SWE_DIV(ustar, hrA - hlB);
     *lw = SWE_DIV(g.lmin, fabs(cor) + smax(kTol, smax(al, ar)));
     // u* <= 0: the right star state, else the left one.  The side is picked
     // first and the shared formula evaluated once, so a warp whose edges take
     // both sides issues it once (the operations per side are the reference's).
     const bool right = !dgt0(ustar);
     const double hx = right ? hr : hl, ux = right ? R.u : L.u, vx = right ? R.v : L.v;
-    const double ax = right ? ar : al, unx = right ? ur : ul;
+    const double ax = right ? ar : al, hxa = right ? hrA : hlB;  // hx (ax - u_n,x)
     const double vt = ux * g.tx + vx * g.ty;  // tangential velocity of that side
     double Ux[3] = {hx, hx * ux, hx * vx};
     double us = vt * g.tx + ustar * g.ty;
     double vs = vt * g.nx + ustar * g.ny;
-    double hs = SWE_DIV(hx * (ax - unx), ax - ustar);
+    double hs = SWE_DIV(hxa, ax - ustar);
     double Us[3] = {hs, hs * us, hs * vs};
     double Fx[3];
     elem_flux(g.nx, g.ny, Ux[0], Ux[1], Ux[2], Fx);
