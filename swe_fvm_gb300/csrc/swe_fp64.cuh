@@ -94,7 +94,11 @@ __device__ __forceinline__ double ddiv_rn(double a, double b) {
   using namespace fp64detail;
   const unsigned long long ua = bits(a), ub = bits(b);
   const unsigned ea = (unsigned)(ua >> 52) & 0x7FFu, eb = (unsigned)(ub >> 52) & 0x7FFu;
-  if (ea - 1u >= 2046u || eb - 1u >= 2046u) return ddiv_hw(a, b);
+  if (ea - 1u >= 2046u || eb - 1u >= 2046u) {
+    // +-0 / normal (still water: zero momentum over a depth) stays in line
+    if ((ua << 1) == 0ull && eb - 1u < 2046u) return from_bits((ua ^ ub) & 0x8000000000000000ull);
+    return ddiv_hw(a, b);
+  }
   unsigned long long ma = (ua & kM52) | kHid;
   const unsigned long long mb = (ub & kM52) | kHid;
   const unsigned long long sign = (ua ^ ub) & 0x8000000000000000ull;
@@ -150,7 +154,7 @@ __device__ __forceinline__ double dsqrt_rn(double x) {
   using namespace fp64detail;
   const unsigned long long ux = bits(x);
   const unsigned ex = (unsigned)(ux >> 52) & 0x7FFu;
-  if (ex - 1u >= 2046u || (ux >> 63)) return dsqrt_hw(x);
+  if (ex - 1u >= 2046u || (ux >> 63)) return (ux << 1) == 0ull ? x : dsqrt_hw(x);  // sqrt(+-0) = +-0 (dry side)
   unsigned long long M = (ux & kM52) | kHid;
   int e = (int)ex - 1023;  // x = M 2^(e - 52)
   if (e & 1) {             // make e - 52 even

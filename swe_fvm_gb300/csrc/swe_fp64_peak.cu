@@ -86,7 +86,11 @@ __device__ double make_operand(unsigned long long r, unsigned long long r2) {
     case 4: exp = 1 + ((r2 >> 16) % 2046); break;                                               // full normal range
     case 5: exp = 1 + ((r2 >> 16) % 60); break;                                                 // near underflow
     case 6: exp = 2046 - ((r2 >> 16) % 60); break;                                              // near overflow
-    default: exp = 1023 + ((r2 >> 16) % 5) - 2; man = (r2 >> 20) & ((1ull << 52) - 1ull); break;
+    default:
+      if (((r2 >> 40) & 3u) == 0u) return __longlong_as_double((long long)(sign << 63));  // +-0
+      exp = 1023 + ((r2 >> 16) % 5) - 2;
+      man = (r2 >> 20) & ((1ull << 52) - 1ull);
+      break;
   }
   return __longlong_as_double((long long)((sign << 63) | (exp << 52) | man));
 }
