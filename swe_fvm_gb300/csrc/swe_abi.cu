@@ -242,7 +242,8 @@ swe_status swe_step(swe_ctx* ctx, int32_t scheme, double dt) {
   if (scheme < 0 || scheme > 2) return fail(&ctx->err, SWE_ERR_INVALID_ARGUMENT, "scheme must be 0, 1 or 2");
   if (!(dt > 0.) || !std::isfinite(dt)) return fail(&ctx->err, SWE_ERR_INVALID_ARGUMENT, "dt must be positive and finite");
   cudaError_t e = cudaMemcpyAsync(ctx->eng.d_fixed_dt, &dt, sizeof(double), cudaMemcpyHostToDevice, ctx->eng.stream());
-  if (e == cudaSuccess) e = ctx->eng.step(scheme, 2);
+  // one replay of the step's CUDA graph (captured on first use)
+  if (e == cudaSuccess) e = ctx->eng.run_graph(scheme, 2, 1);
   if (e != cudaSuccess) return cuda_fail(&ctx->err, e, "swe_step");
   return SWE_OK;
   SWE_GUARD_END(&ctx->err)
