@@ -86,6 +86,24 @@ __global__ void k_seed_gauges(double* lamw, const int* g, int n, const double* g
   if (q < n) atomicAdd(lamw + g[q], grad[q]);
 }
 
+// the gauge seeds of step n = *s0 + loc, when it ends an observation window
+__global__ void k_seed_gauges_seg(double* lamw, const int* g, int n_g, const double* tg, const long long* s0,
+                                  long long loc, long long obs) {
+  const long long n = *s0 + loc;
+  if ((n + 1) % obs != 0) return;
+  const long long j = (n + 1) / obs - 1;
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < n_g) atomicAdd(lamw + g[q], tg[j * n_g + q]);
+}
+
+// *dst = dts[*s0 + loc]: the recorded dt of a step of the current segment
+__global__ void k_fetch_dt(double* dst, const double* dts, const long long* s0, long long loc) {
+  if (threadIdx.x == 0) *dst = dts[*s0 + loc];
+}
+__global__ void k_set_i64(long long* dst, long long v) {
+  if (threadIdx.x == 0) *dst = v;
+}
+
 // ---------------------------------------------------------------- R1: update
 // nst: the stage's conservative state before ConsAssigner ([3][C], kept by the
 // segment recompute), or null to recompute it from the stage's fluxes.
@@ -965,15 +983,21 @@ std::string Engine::adjoint_forward(int scheme, int64_t n_steps, int64_t ckpt, c
     return "tape allocation failed";
   if (cudaMalloc(&a.d_gauges, (n_gauges ? n_gauges : 1) * sizeof(int)) != cudaSuccess) return "tape allocation failed";
   cudaMemcpy(a.d_gauges, gauges, n_gauges * sizeof(int), cudaMemcpyHostToDevice);
+  // every checkpoint allocated up front (no allocation inside the run)
+  const int64_t n_ckpt = n_steps > 0 ? (n_steps + ckpt - 1) / ckpt : 0;
+  for (int64_t q = 0; q < n_ckpt; ++q) {
+    double* cp = nullptr;
+    if (cudaMalloc(&cp, 3 * C * sizeof(double)) != cudaSuccess) return "checkpoint allocation failed";
+    a.checkpoints.push_back(cp);
+  }
   for (int64_t n = 0; n < n_steps; ++n) {
     if (n % ckpt == 0) {
-      double* cp = nullptr;
-      if (cudaMalloc(&cp, 3 * C * sizeof(double)) != cudaSuccess) return "checkpoint allocation failed";
-      a.checkpoints.push_back(cp);
+      double* cp = a.checkpoints[n / ckpt];
       for (int q = 0; q < 3; ++q)
         cudaMemcpyAsync(cp + q * C, state(0, q), C * sizeof(double), cudaMemcpyDeviceToDevice, stream_);
     }
-    cudaError_t e = step(scheme, 1);
+    // the plain step's CUDA graph (dt = CFLdt() of the previous flux pass)
+    cudaError_t e = run_graph(scheme, 1, 1);
     if (e != cudaSuccess) return std::string("forward step: ") + cudaGetErrorString(e);
     cudaMemcpyAsync(a.d_dt + n, work_.dt, sizeof(double), cudaMemcpyDeviceToDevice, stream_);
     if (obs > 0 && (n + 1) % obs == 0 && n_gauges > 0) {
@@ -1086,16 +1110,18 @@ std::string Engine::adjoint_backward(const double* trace_grads_host, double* gra
   cudaMemsetAsync(lam_step, 0, 3 * C * sizeof(double), stream_);
   std::string err;
   const int64_t nseg = (a.n_steps + K - 1) / K;
-  for (int64_t seg = nseg - 1; seg >= 0 && err.empty(); --seg) {
-    const int64_t s0 = seg * K, s1 = std::min(a.n_steps, s0 + K);
-    // recompute the segment stage by stage with the recorded dt, keeping every
-    // stage's forward intermediates when they fit
-    for (int q = 0; q < 3; ++q)
-      cudaMemcpyAsync(store[0] + q * C, a.checkpoints[seg] + q * C, C * sizeof(double), cudaMemcpyDeviceToDevice,
-                      stream_);
-    for (int64_t n = s0; n < s1; ++n) {
-      const int64_t base = (n - s0) * ns;
-      cudaMemcpyAsync(d_fixed_dt, a.d_dt + n, sizeof(double), cudaMemcpyDeviceToDevice, stream_);
+  // The first step index of the current segment lives on the device, so that
+  // one captured graph of a full segment's recompute and one of its reverse
+  // replay for every full segment.
+  long long* d_s0 = nullptr;
+  if (cudaMalloc(&d_s0, sizeof(long long)) != cudaSuccess) err = "allocation failed";
+  const bool seeds = a.obs > 0 && a.n_gauges > 0;
+  // recompute of steps s0 .. s0+len-1 with the recorded dt, keeping every
+  // stage's forward intermediates when they fit
+  auto enqueue_recompute = [&](int64_t len) -> cudaError_t {
+    for (int64_t loc = 0; loc < len; ++loc) {
+      const int64_t base = loc * ns;
+      k_fetch_dt<<<1, 32, 0, stream_>>>(d_fixed_dt, a.d_dt, d_s0, loc);
       double* S0p = store[base];
       const double* u0[3] = {S0p, S0p + C, S0p + 2 * C};
       for (int s = 0; s < ns; ++s) {
@@ -1108,8 +1134,19 @@ std::string Engine::adjoint_backward(const double* trace_grads_host, double* gra
           const DevWork saved = work_;
           work_ = kept[base + s];
           e = reset_pass();
-          if (e == cudaSuccess) e = interface_values(in[0], in[1], in[2], s == 0 ? 2 : 0);
-          if (e == cudaSuccess) e = fluxes(in[0]);
+          if (e == cudaSuccess) {
+            // the plain stage's kernels with PartWet2 and the fluxes next to
+            // partially-wet cells on the side stream, keeping every
+            // intermediate (k_drain_keep leaves the node maxima and the list)
+            launch_recon1(in[0], in[1], in[2], s == 0 ? 2 : 0);
+            cudaEventRecord(ev_fork_, stream_);
+            cudaStreamWaitEvent(side_, ev_fork_, 0);
+            launch_recon2(in[0], in[1], in[2], side_);
+            fluxes_pw(in[0], side_);
+            cudaEventRecord(ev_join_, side_);
+            e = fluxes(in[0], 1);
+            cudaStreamWaitEvent(stream_, ev_join_, 0);
+          }
           if (e == cudaSuccess) {
             k_drain_keep<<<gc, b, 0, stream_>>>(mesh_, work_, in[0]);
             e = update_only(sc.s[s], in, u0, out, kept_n[base + s]);
@@ -1119,23 +1156,19 @@ std::string Engine::adjoint_backward(const double* trace_grads_host, double* gra
           e = reset_pass();
           if (e == cudaSuccess) e = launch_stage(sc.s[s], in, u0, out, s == 0, s == 0 ? 2 : 0);
         }
-        if (e != cudaSuccess) {
-          err = std::string("segment recompute: ") + cudaGetErrorString(e);
-          break;
-        }
+        if (e != cudaSuccess) return e;
       }
-      if (!err.empty()) break;
     }
-    if (!err.empty()) break;
-    // reverse the steps of the segment
-    for (int64_t n = s1 - 1; n >= s0; --n) {
-      const int64_t base = (n - s0) * ns;
-      if (a.obs > 0 && (n + 1) % a.obs == 0 && a.n_gauges > 0) {
-        const int64_t j = (n + 1) / a.obs - 1;
-        k_seed_gauges<<<(a.n_gauges + 255) / 256, 256, 0, stream_>>>(lam_step, a.d_gauges, a.n_gauges,
-                                                                     d_tg + j * a.n_gauges);
-      }
-      cudaMemcpyAsync(work_.dt, a.d_dt + n, sizeof(double), cudaMemcpyDeviceToDevice, stream_);
+    return cudaGetLastError();
+  };
+  // reverse of steps s0+len-1 .. s0
+  auto enqueue_reverse = [&](int64_t len) -> cudaError_t {
+    for (int64_t loc = len - 1; loc >= 0; --loc) {
+      const int64_t base = loc * ns;
+      if (seeds)
+        k_seed_gauges_seg<<<(a.n_gauges + 255) / 256, 256, 0, stream_>>>(lam_step, a.d_gauges, a.n_gauges, d_tg,
+                                                                         d_s0, loc, a.obs);
+      k_fetch_dt<<<1, 32, 0, stream_>>>(work_.dt, a.d_dt, d_s0, loc);
       double* S0p = store[base];
       const double* u0[3] = {S0p, S0p + C, S0p + 2 * C};
       cudaMemsetAsync(w.lam0, 0, 3 * C * sizeof(double), stream_);
@@ -1146,18 +1179,57 @@ std::string Engine::adjoint_backward(const double* trace_grads_host, double* gra
         cudaMemsetAsync(w.lamp, 0, 3 * C * sizeof(double), stream_);
         cudaError_t e = keep ? adjoint_stage_reverse_stored(sc.s[s], in, u0, w, kept[base + s], kept_n[base + s])
                              : adjoint_stage_reverse(sc.s[s], in, u0, w);
-        if (e != cudaSuccess) {
-          err = std::string("stage reverse: ") + cudaGetErrorString(e);
-          break;
-        }
+        if (e != cudaSuccess) return e;
         k_fold_scatter<<<gc, b, 0, stream_>>>((int)C, w.lamp, w.lscatter);
         cudaMemcpyAsync(w.lam, w.lamp, 3 * C * sizeof(double), cudaMemcpyDeviceToDevice, stream_);
       }
-      if (!err.empty()) break;
       // adjoint of the step's initial state: through the first stage's input and the Shu-Osher terms
       k_add3<<<gc, b, 0, stream_>>>((int)C, w.lam, w.lam0, lam_step);
     }
+    return cudaGetLastError();
+  };
+  // captures body() on a private stream; null graph if capture fails
+  auto capture = [&](auto&& body) -> cudaGraphExec_t {
+    cudaStream_t cap;
+    if (cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking) != cudaSuccess) return nullptr;
+    const cudaStream_t saved = stream_;
+    stream_ = cap;
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t ge = nullptr;
+    if (cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+      const cudaError_t e = body();
+      const cudaError_t e2 = cudaStreamEndCapture(cap, &g);
+      if (e == cudaSuccess && e2 == cudaSuccess && cudaGraphInstantiate(&ge, g, 0) != cudaSuccess) ge = nullptr;
+      if (g) cudaGraphDestroy(g);
+    }
+    stream_ = saved;
+    cudaStreamDestroy(cap);
+    cudaGetLastError();
+    return ge;
+  };
+  cudaGraphExec_t g_rec = nullptr, g_rev = nullptr;
+  bool tried = false;
+  for (int64_t seg = nseg - 1; seg >= 0 && err.empty(); --seg) {
+    const int64_t s0 = seg * K, s1 = std::min(a.n_steps, s0 + K), len = s1 - s0;
+    for (int q = 0; q < 3; ++q)
+      cudaMemcpyAsync(store[0] + q * C, a.checkpoints[seg] + q * C, C * sizeof(double), cudaMemcpyDeviceToDevice,
+                      stream_);
+    k_set_i64<<<1, 32, 0, stream_>>>(d_s0, s0);
+    if (len == K && !tried) {
+      tried = true;
+      g_rec = capture([&] { return enqueue_recompute(K); });
+      g_rev = capture([&] { return enqueue_reverse(K); });
+    }
+    cudaError_t e = (len == K && g_rec) ? cudaGraphLaunch(g_rec, stream_) : enqueue_recompute(len);
+    if (e != cudaSuccess) {
+      err = std::string("segment recompute: ") + cudaGetErrorString(e);
+      break;
+    }
+    e = (len == K && g_rev) ? cudaGraphLaunch(g_rev, stream_) : enqueue_reverse(len);
+    if (e != cudaSuccess) err = std::string("stage reverse: ") + cudaGetErrorString(e);
   }
+  if (g_rec) cudaGraphExecDestroy(g_rec);
+  if (g_rev) cudaGraphExecDestroy(g_rev);
   (void)lam_cur;
   if (err.empty()) {
     double* d_out = store[0];
@@ -1172,6 +1244,7 @@ std::string Engine::adjoint_backward(const double* trace_grads_host, double* gra
   for (auto& p : store) cudaFree(p);
   cudaFree(d_tg);
   cudaFree(lam_step);
+  cudaFree(d_s0);
   return err;
 }
 
