@@ -344,52 +344,22 @@ struct P1 {
   bool kept;
   double w0;
 };
-// pwrec: the PartWet1 levels the forward pass 1 stored for its partially-wet
-// cells (read instead of repeating the cubic solve).
-__device__ P1 pass1(const DevMesh& m, const double* W, int c, const double* pwrec) {
-  P1 r{0, 0, false, 0.};
-  const int C = m.C;
-  const double w = W[c];
-  const double h = w - m.bc[c];
-  if (!is_wet(h)) return r;
-  if (!dlt(m.fwthr[c], w)) {
-    r.type = 1;
-    r.w0 = pwrec[c];
-    return r;
-  }
-  r.type = 2;
-  r.w0 = w;
-  bool first_order = false;
-  double wn[3];
-  for (int k = 0; k < 3; ++k) {
-    const int nb = m.cnbr[k * C + c];
-    const double wj = W[nb];
-    wn[k] = wj;
-    if (dlt(m.fwthr[nb], wj)) {
-    } else if (!is_wet(wj - m.bc[nb])) {
-      first_order = true;
-    } else {
-      r.mask |= 1 << k;
-    }
-  }
-  if (first_order) return r;
-  const double* rec = m.combo + ((size_t)c * 8 + r.mask) * kComboStride;
-  for (int k = 0; k < 3; ++k)
-    if (!is_wet((rec[2 + k] + w) - m.zn[k * C + c])) return r;
-  for (int k = 0; k < 3; ++k) {
-    const double vek = w + rec[5 + k];
-    if (!(dle(smin(w, wn[k]), vek) && dle(vek, smax(w, wn[k])))) return r;
-  }
-  r.kept = true;
+__device__ P1 pass1(const DevWork& wk, const double* W, int c) {
+  // the class the forward pass 1 stored; the level of a partially-wet cell is
+  // its PartWet1 level, of a fully-wet cell its own w
+  const unsigned cl = wk.cls[c];
+  P1 r{(int)(cl & 3u), (int)((cl >> 2) & 7u), ((cl >> 5) & 1u) != 0u, 0.};
+  if (r.type == 1) r.w0 = wk.pwrec[c];
+  else if (r.type == 2) r.w0 = W[c];
   return r;
 }
 
 // Pass-1 value of cell c at its local node kn (AtPoint(P).w), and where its
 // derivative goes: dstate = d value / d W[c]; static part to node z.
-__device__ double pass1_node_value(const DevMesh& m, const double* W, int c, int kn, const double* pwrec) {
+__device__ double pass1_node_value(const DevMesh& m, const DevWork& wk, const double* W, int c, int kn) {
   const int C = m.C;
   const double z = m.zn[kn * C + c];
-  const P1 p = pass1(m, W, c, pwrec);
+  const P1 p = pass1(wk, W, c);
   if (p.type == 0) return m.dry[(size_t)c * kDryStride + kn];
   double off = 0.;
   if (p.type == 2 && p.kept) off = m.combo[((size_t)c * 8 + p.mask) * kComboStride + 8 + kn];
@@ -489,6 +459,7 @@ __device__ bool partwet2_t(const Pw2Rec& r, const T& w, const T& w23, const T& z
 // adjoints of the slot (w, u, v, sx, sy) and the forward inputs of AtPoint,
 // returns adjoints of (w0 + off) [law], u0, v0, gx, gy, and of the slot's
 // edge bathymetry (ze).
+template <bool COR0>
 __device__ void slot_reverse(double ze, double a_w, double u0, double v0, double cor, double lw, double lu, double lv,
                              double lsx, double lsy, double* law, double* lu0, double* lv0, double* lgx, double* lgy,
                              double* lze) {
@@ -503,7 +474,11 @@ __device__ void slot_reverse(double ze, double a_w, double u0, double v0, double
     av = 0.;
   }
   // src += cor (-v, u) uses the assigned velocities
-  double lue = lu + cor * lsy, lve = lv - cor * lsx;
+  double lue = lu, lve = lv;
+  if (!COR0) {
+    lue = fma(cor, lsy, lu);
+    lve = fma(-cor, lsx, lv);
+  }
   double law_ = 0., lau = 0., lav = 0., lz = 0.;
   const double h = aw_ - ze;
   if (!is_wet(h)) {
@@ -578,6 +553,28 @@ __device__ void combo_points_to_nodes(const DevMesh& m, AdjWork& aw, int c, int 
   }
 }
 
+// the plane-point adjoint table of every cell and neighbour combination
+__global__ void k_plane_adj_init(DevMesh m, double* padj) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.C) return;
+  double* out = padj + (size_t)c * 48;
+  bool interior = true;
+  for (int k = 0; k < 3; ++k) interior = interior && m.cnbr[k * m.C + c] >= 0;
+  for (int q = 0; q < 8; ++q) {
+    double lx[3] = {0., 0., 0.}, ly[3] = {0., 0., 0.};
+    if (interior) {
+      double px[3], py[3];
+      combo_plane_points(m, c, q, px, py);
+      plane_points_adjoint(px, py, 1., 0., lx);
+      plane_points_adjoint(px, py, 0., 1., ly);
+    }
+    for (int k = 0; k < 3; ++k) {
+      out[q * 6 + k] = lx[k];
+      out[q * 6 + 3 + k] = ly[k];
+    }
+  }
+}
+
 // Forward-only part of a partially-wet cell's reverse: the PartWet2 plane (or
 // PartWet1 level) with its derivatives, and where the PartWet2 node maximum
 // w23 came from.  It reads no adjoint, so it runs beside R1-R3.
@@ -631,14 +628,14 @@ __device__ void pw_jacobian(const DevMesh& m, const DevWork& wk, const AdjWork& 
   int best = -1, bestk = 0;
   for (int q = aw.node_ptr[nd]; q < aw.node_ptr[nd + 1]; ++q) {
     const int c = aw.node_cells[q] >> 2, kn = aw.node_cells[q] & 3;
-    if (pass1_node_value(m, W, c, kn, wk.pwrec) == w23) {
+    if (pass1_node_value(m, wk, W, c, kn) == w23) {
       best = c;
       bestk = kn;
       break;
     }
   }
   if (best >= 0) {
-    const P1 pc = pass1(m, W, best, wk.pwrec);
+    const P1 pc = pass1(wk, W, best);
     const double zc_ = m.zn[bestk * C + best];
     J.route = 0;
     J.target = cnode(m, best, bestk);
@@ -668,9 +665,9 @@ __device__ void pw_jacobian(const DevMesh& m, const DevWork& wk, const AdjWork& 
           J.route = 2;
           if (pc.kept) {
             const Pw2Rec& rb = m.pw2[best];
-            double px[3], py[3];
-            combo_plane_points(m, best, pc.mask, px, py);
-            plane_points_adjoint(px, py, rb.dnode[bestk][0], rb.dnode[bestk][1], J.rc);
+            const double* T = aw.padj + (size_t)best * 48 + pc.mask * 6;
+            const double dx = rb.dnode[bestk][0], dy = rb.dnode[bestk][1];
+            for (int k = 0; k < 3; ++k) J.rc[k] = fma(dx, T[k], dy * T[3 + k]);
             J.mask = pc.mask;
           }
         } else {
@@ -688,6 +685,7 @@ __device__ void pw_jacobian(const DevMesh& m, const DevWork& wk, const AdjWork& 
 
 // Reverse of the reconstruction of cell i; partially-wet cells contract the
 // Jacobians pw_jacobian stored for them.
+template <bool COR0>
 __device__ void adj_recon_cell(const DevMesh& m, const DevWork& wk, AdjWork aw, const double* W, const double* U,
                                const double* V, int i, int batched) {
   const int C = m.C;
@@ -705,7 +703,7 @@ __device__ void adj_recon_cell(const DevMesh& m, const DevWork& wk, AdjWork aw, 
       lbc -= lh;
     }
   }
-  const P1 p = pass1(m, W, i, wk.pwrec);
+  const P1 p = pass1(wk, W, i);
   if (p.type == 0) {
     const double* dr = m.dry + (size_t)i * kDryStride;
     // interface values (dew_k, 0, 0) and slope (sx, sy) are functions of the
@@ -723,7 +721,7 @@ __device__ void adj_recon_cell(const DevMesh& m, const DevWork& wk, AdjWork aw, 
     for (int k = 0; k < 3; ++k) {
       const int slot = k * C + i;
       double law, lu0, lv0, lgx, lgy, lze;
-      slot_reverse(m.ze[slot], dr[3 + k], 0., 0., cor, aw.lew[slot], aw.leu[slot], aw.lev[slot], aw.lsx[slot],
+      slot_reverse<COR0>(m.ze[slot], dr[3 + k], 0., 0., cor, aw.lew[slot], aw.leu[slot], aw.lev[slot], aw.lsx[slot],
                    aw.lsy[slot], &law, &lu0, &lv0, &lgx, &lgy, &lze);
       const D e0v = bcd + (sxd * r.dedge[k][0] + syd * r.dedge[k][1]);
       for (int q = 0; q < 3; ++q) lz3[q] = fma(law, e0v.d[q], fma(lgx, sxd.d[q], fma(lgy, syd.d[q], lz3[q])));
@@ -759,7 +757,7 @@ __device__ void adj_recon_cell(const DevMesh& m, const DevWork& wk, AdjWork aw, 
   for (int k = 0; k < 3; ++k) {
     const int slot = k * C + i;
     double law, lu0, lv0, lgxk, lgyk, lze;
-    slot_reverse(m.ze[slot], w0 + off[k], u, v, cor, aw.lew[slot], aw.leu[slot], aw.lev[slot], aw.lsx[slot],
+    slot_reverse<COR0>(m.ze[slot], w0 + off[k], u, v, cor, aw.lew[slot], aw.leu[slot], aw.lev[slot], aw.lsx[slot],
                  aw.lsy[slot], &law, &lu0, &lv0, &lgxk, &lgyk, &lze);
     lw0 += law;
     loff[k] = law;
@@ -780,9 +778,8 @@ __device__ void adj_recon_cell(const DevMesh& m, const DevWork& wk, AdjWork aw, 
         lg0 = fma(loff[k], r.dedge[k][0], lg0);
         lg1 = fma(loff[k], r.dedge[k][1], lg1);
       }
-      double px[3], py[3], lp[3];
-      combo_plane_points(m, i, p.mask, px, py);
-      plane_points_adjoint(px, py, lg0, lg1, lp);
+      const double* T = aw.padj + (size_t)i * 48 + p.mask * 6;
+      const double lp[3] = {fma(lg0, T[0], lg1 * T[3]), fma(lg0, T[1], lg1 * T[4]), fma(lg0, T[2], lg1 * T[5])};
       combo_points_to_nodes(m, aw, i, p.mask, lp);
     }
   } else if (!J->plane) {
@@ -833,10 +830,11 @@ __device__ void adj_recon_cell(const DevMesh& m, const DevWork& wk, AdjWork aw, 
   lam_cell_z(m, aw, i, lbc);
 }
 
+template <bool COR0>
 __global__ void __launch_bounds__(256) k_adj_recon(DevMesh m, DevWork wk, AdjWork aw, const double* W,
                                                    const double* U, const double* V, int batched) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < m.C) adj_recon_cell(m, wk, aw, W, U, V, i, batched);
+  if (i < m.C) adj_recon_cell<COR0>(m, wk, aw, W, U, V, i, batched);
 }
 
 // Jacobians of the stage's partially-wet cells (the list pass 1 of the forward
@@ -910,6 +908,8 @@ std::string Engine::adjoint_init() {
   A(w.lF0, 3 * C); A(w.lF1, 3 * C); A(w.lF2, 3 * C); A(w.lF0d, 3 * C); A(w.ldtk, 3 * C); A(w.lhwall, 3 * C);
   A(w.lbc, C); A(w.lscatter, C); A(w.lz, N);
   w.pwjac = a->alloc<PwJac>(C);
+  w.padj = a->alloc<double>(48 * C);
+  ok = ok && w.pwjac && w.padj;
   w.route = a->alloc<unsigned char>(3 * C);
   ok = ok && w.route;
   // twin slots, node -> cells, edge nodes (host, from the instance's topology)
@@ -955,6 +955,11 @@ std::string Engine::adjoint_init() {
   w.node_cells = d_cells;
   w.edge_nodes = d_en;
   cudaMemset(w.lscatter, 0, C * sizeof(double));
+  k_plane_adj_init<<<(int)((C + 255) / 256), 256, 0, stream_>>>(mesh_, w.padj);
+  if (cudaStreamSynchronize(stream_) != cudaSuccess) {
+    delete a;
+    return "adjoint table set-up failed";
+  }
   if (cudaStreamCreateWithFlags(&a->side, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreateWithFlags(&a->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&a->ev_join, cudaEventDisableTiming) != cudaSuccess) {
@@ -1058,7 +1063,7 @@ std::string Engine::adjoint_backward(const double* trace_grads_host, double* gra
   // draining dt, node maxima, part-wet list) when device memory allows
   const int64_t E = mesh_.E;
   const size_t per_stage = ((15 * C + 3 * E + 5 * C) * sizeof(double) + N * sizeof(unsigned long long) +
-                            (C + 1) * sizeof(int) + 255) / 256 * 256;
+                            (C + 1) * sizeof(int) + C + 255) / 256 * 256;
   size_t free_b = 0, total_b = 0;
   cudaMemGetInfo(&free_b, &total_b);
   const bool keep = (double)per_stage * (double)(K * ns) < 0.6 * (double)free_b;
@@ -1095,6 +1100,7 @@ std::string Engine::adjoint_backward(const double* trace_grads_host, double* gra
       wq.pwlist = (int*)take(C * sizeof(int));
       kept_n[q] = (double*)take(3 * C * sizeof(double));
       wq.pwcount = (int*)take(sizeof(int));
+      wq.cls = (unsigned char*)take((size_t)C);
       kept[q] = wq;
     }
   }
@@ -1284,7 +1290,8 @@ cudaError_t Engine::adjoint_stage_reverse_stored(const Stage& st, const double* 
     default: k_adj_flux<1, 2><<<ge, b, 0, stream_>>>(mesh_, wk, aw, in[0]); break;
   }
   cudaStreamWaitEvent(stream_, a.ev_join, 0);
-  k_adj_recon<<<gc, b, 0, stream_>>>(mesh_, wk, aw, in[0], in[1], in[2], batched_);
+  if (cor0_) k_adj_recon<true><<<gc, b, 0, stream_>>>(mesh_, wk, aw, in[0], in[1], in[2], batched_);
+  else k_adj_recon<false><<<gc, b, 0, stream_>>>(mesh_, wk, aw, in[0], in[1], in[2], batched_);
   launches_ += 5;
   return cudaGetLastError();
 }

@@ -37,6 +37,10 @@ struct AdjWork {
   const int* node_cells;                      // (cell << 2) | local node index
   const int* edge_nodes;                      // [2E] global node ids of each edge
   PwJac* pwjac;                               // [C] partially-wet cells' Jacobians
+  // [C][8][6] adjoint of the fully-wet combination plane's point z: for
+  // neighbour mask q, lp_k = lg0 padj[.][q][k] + lg1 padj[.][q][3 + k]
+  // (geometry only; zero for cells next to a wall, which are never fully wet)
+  double* padj;
 };
 
 }  // namespace swe

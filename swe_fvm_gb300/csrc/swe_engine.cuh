@@ -96,7 +96,9 @@ struct DevWork {
   int* pwlist;                 // [C] partially-wet cells of this stage
   int* pwcount;                // [1]
   double* pwrec;               // [C] PartWet1 level of listed cells
-  unsigned char* pwflag;       // [C] 1 for the stage's partially-wet cells (pass 1)
+  // [C] pass-1 class of each cell: type (0 dry, 1 partially wet, 2 fully wet)
+  // | neighbour combination mask << 2 | combination plane kept << 5
+  unsigned char* cls;
   unsigned long long* r;       // [I] ordered key of min length-to-wavespeed
   double* dt;                  // [I] step dt
   double* tsum;                // [I] accumulated time

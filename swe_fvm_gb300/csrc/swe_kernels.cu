@@ -122,6 +122,7 @@ __global__ void __launch_bounds__(256) k_recon1(DevMesh m, DevWork wk, const dou
                                                 int latch_mode) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   bool part = false;
+  unsigned char cls = 0;  // dry unless set below
   if (i < m.C) {
     const int inst = BATCH ? m.cinst[i] : 0;
     if (i == (BATCH ? m.inst_cell_begin[inst] : 0)) {
@@ -162,6 +163,7 @@ __global__ void __launch_bounds__(256) k_recon1(DevMesh m, DevWork wk, const dou
         node_max(wk, m.cnode[k * C + i], val, z);
       }
       part = true;
+      cls = 1;
     } else {
       // ReconstructFullWetCell (src/MUSCLObject.cpp:38-84)
       int mask = 0;
@@ -180,6 +182,7 @@ __global__ void __launch_bounds__(256) k_recon1(DevMesh m, DevWork wk, const dou
           mask |= 1 << k;  // partially-wet neighbour: plane point at the edge centre
         }
       }
+      cls = (unsigned char)(2 | (mask << 2));
       double gx = 0., gy = 0.;
       double toff[3] = {0., 0., 0.}, noff[3] = {0., 0., 0.};
       if (!first_order) {
@@ -201,6 +204,7 @@ __global__ void __launch_bounds__(256) k_recon1(DevMesh m, DevWork wk, const dou
             if (!(dle(vmin, vek) && dle(vek, vmax))) tvd = false;
           }
           if (tvd) {
+            cls |= 32;  // combination plane kept
             gx = g0;
             gy = g1;
 #pragma unroll
@@ -228,7 +232,7 @@ __global__ void __launch_bounds__(256) k_recon1(DevMesh m, DevWork wk, const dou
       }
     }
   }
-  if (i < m.C) wk.pwflag[i] = part ? 1 : 0;
+  if (i < m.C) wk.cls[i] = cls;
   // warp-aggregated append of the partially-wet cells
   const unsigned bal = __ballot_sync(0xffffffffu, part);
   if (bal) {
@@ -358,7 +362,7 @@ __global__ void __launch_bounds__(256) k_flux(DevMesh m, DevWork wk, const doubl
     bool mine = true;
     if (MODE == 1) {
       const int nb = m.enb[e];
-      mine = !(wk.pwflag[m.eown[e]] | (nb >= 0 ? wk.pwflag[nb] : (unsigned char)0));
+      mine = !(((wk.cls[m.eown[e]] & 3) == 1) || (nb >= 0 && (wk.cls[nb] & 3) == 1));
     }
     if (mine) flux_edge<FLUX>(m, wk, W, e, inst, &lw);
   }
@@ -418,7 +422,7 @@ __global__ void __launch_bounds__(128) k_flux_pw(DevMesh m, DevWork wk, const do
     const int i = wk.pwlist[q];
     const int e = m.cedge[k * C + i];
     const int o = m.eown[e];
-    if ((wk.pwflag[o] ? o : m.enb[e]) != i) continue;
+    if ((((wk.cls[o] & 3) == 1) ? o : m.enb[e]) != i) continue;
     const int inst = BATCH ? m.einst[e] : 0;
     double lw = kInf;
     flux_edge<FLUX>(m, wk, W, e, inst, &lw);
@@ -648,7 +652,7 @@ std::string Engine::init(std::vector<HostInstance>&& inst, int flux, int ws, int
   Wk.pwlist = dalloc<int>(C);
   Wk.pwcount = dalloc<int>(1);
   Wk.pwrec = dalloc<double>(C);
-  Wk.pwflag = dalloc<unsigned char>(C);
+  Wk.cls = dalloc<unsigned char>(C);
   Wk.r = dalloc<unsigned long long>(I);
   Wk.dt = dalloc<double>(I);
   Wk.tsum = dalloc<double>(I);
@@ -659,7 +663,7 @@ std::string Engine::init(std::vector<HostInstance>&& inst, int flux, int ws, int
   d_io = dalloc<double>(3 * C);
   d_ioflag = dalloc<unsigned>(1);
   if (!Wk.ew || !Wk.eu || !Wk.ev || !Wk.sx || !Wk.sy || !Wk.f0 || !Wk.f1 || !Wk.f2 || !Wk.drain || !Wk.maxwp ||
-      !Wk.pwlist || !Wk.pwcount || !Wk.pwrec || !Wk.pwflag || !Wk.r || !Wk.dt || !Wk.tsum || !d_fixed_dt || !Wk.err ||
+      !Wk.pwlist || !Wk.pwcount || !Wk.pwrec || !Wk.cls || !Wk.r || !Wk.dt || !Wk.tsum || !d_fixed_dt || !Wk.err ||
       !state_[5] || !d_io || !d_ioflag) {
     *st = 6;
     return "device allocation failed";
