@@ -245,7 +245,8 @@ def run_gpu(args):
     _lib.check(L.swe_measure_fp64_peak(ctypes.byref(fp64)))
     hbm, src = peaks()
     achieved = BYTES_PER_CELL_STEP * C / (ms_step * 1e-3) / 1e9
-    roof = {"bound": "hbm", "kernel": "ssprk2_step (2 stages x 5 kernels, one CUDA graph)", "achieved": achieved,
+    roof = {"bound": "hbm", "kernel": "ssprk2_step (one CUDA graph: 2 stages x 6 kernels on two streams)",
+            "achieved": achieved,
             "peak": hbm, "unit": "GB/s", "frac": achieved / hbm, "peak_source": src,
             "algorithmic_bytes_per_launch": BYTES_PER_CELL_STEP * C,
             "traffic": TRAFFIC_PER_STEP.get(LATTICE),
@@ -395,9 +396,10 @@ def run_adjoint(torch, stream):
             "config": {"workload": "adjoint_250k", "flux": "HLLC+Einfeldt", "scheme": "SSPRK2", "cfl": 0.15}}
 
 
-# DRAM bytes per SSPRK2 step from the ncu launch capture (sum over the step's
-# 10 kernels); filled from the committed profile summary.
-TRAFFIC_PER_STEP = {}
+# DRAM bytes per SSPRK2 step (dram__bytes_read.sum + dram__bytes_write.sum over
+# the step's 12 kernels, one ncu launch capture of the 1M-cell mesh, lattice
+# 708, the same command line with --profile).
+TRAFFIC_PER_STEP = {708: 1.739e9}
 
 
 def run_reference(args):
