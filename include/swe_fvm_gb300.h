@@ -248,6 +248,20 @@ swe_status swe_batch_launch_count(swe_batch* b, int64_t* n);
 swe_status swe_batch_synchronize(swe_batch* b);
 const char* swe_batch_last_error(swe_batch* b);
 
+/* The discrete adjoint of a batch: as swe_adjoint_forward / _backward / _dts,
+ * over all instances at once.  Cells, nodes and gauges are numbered over the
+ * concatenation of the instances in creation order (instance q's cell i is
+ * cell i + the cell counts of instances 0..q-1; nodes likewise); each instance
+ * keeps its own CFL dt, recorded per step (dts_out is n_steps x n_instances).
+ * grad_prim0 is 3 x C_total and grad_bathymetry N_total.  No reference
+ * counterpart. */
+swe_status swe_batch_adjoint_forward(swe_batch* b, int32_t scheme, int64_t n_steps, int64_t checkpoint_every,
+                                     int32_t n_gauges, const int64_t* gauge_cells, int64_t obs_every,
+                                     double* traces_out);
+swe_status swe_batch_adjoint_backward(swe_batch* b, const double* trace_grads, double* grad_prim0,
+                                      double* grad_bathymetry);
+swe_status swe_batch_adjoint_dts(swe_batch* b, double* dts_out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -32,7 +32,7 @@ EXPORTS = [
     "swe_get_fluxes", "swe_get_node_max", "swe_time_kernels", "swe_measure_fp64_peak", "swe_selftest_fp64", "swe_selftest_flux_adjoint", "swe_num_cells", "swe_launch_count", "swe_synchronize",
     "swe_last_error", "swe_adjoint_forward", "swe_adjoint_backward", "swe_adjoint_dts", "swe_edge_fluxes_noalloc", "swe_batch_create", "swe_batch_destroy", "swe_batch_set_stream", "swe_batch_run_cfl", "swe_batch_run",
     "swe_batch_get_prim", "swe_batch_time", "swe_batch_launch_count", "swe_batch_synchronize",
-    "swe_batch_last_error",
+    "swe_batch_last_error", "swe_batch_adjoint_forward", "swe_batch_adjoint_backward", "swe_batch_adjoint_dts",
 ]
 
 
@@ -126,6 +126,9 @@ def load(build_if_needed: bool = True):
         "swe_batch_launch_count": [vp, P(i64)],
         "swe_batch_synchronize": [vp],
         "swe_batch_last_error": [vp],
+        "swe_batch_adjoint_forward": [vp, i32, i64, i64, i32, vp, i64, vp],
+        "swe_batch_adjoint_backward": [vp, vp, vp, vp],
+        "swe_batch_adjoint_dts": [vp, vp],
     }
     for name, args in sig.items():
         f = getattr(L, name)

@@ -16,7 +16,7 @@ import numpy as np
 
 from . import _lib
 from .mesh import Mesh
-from .solver import Fluxes, SpaceDisc, Wavespeeds
+from .solver import Batch, Fluxes, SpaceDisc, Wavespeeds
 
 
 class Rollout:
@@ -47,6 +47,50 @@ class Rollout:
         L = _lib.load()
         self.sd._check(L.swe_adjoint_backward(self.sd.ctx, tg.ctypes.data, gp.ctypes.data, gz.ctypes.data))
         return gp, gz
+
+
+class BatchRollout:
+    """The taped forward run and its adjoint for a batch of independent
+    instances: one launch per stage kernel over all of them, each instance with
+    its own CFL dt, gauges and gradients."""
+
+    def __init__(self, meshes, prims, fluxer=None, cfl=0.15, cor=0.0):
+        self.meshes = [m.contiguous() for m in meshes]
+        self.batch = Batch(self.meshes, prims, fluxer=fluxer, cor=cor, cfl=cfl)
+        self.cell_off = np.concatenate([[0], np.cumsum([m.num_cells for m in self.meshes])]).astype(np.int64)
+        self.node_off = np.concatenate([[0], np.cumsum([m.num_nodes for m in self.meshes])]).astype(np.int64)
+        self.gauge_counts = []
+
+    def forward(self, scheme: int, n_steps: int, checkpoint_every: int, gauges, obs_every: int):
+        """gauges: one array of local cell ids per instance.  Returns one
+        (n_steps // obs_every, n_gauges_q) trace array per instance."""
+        self.gauge_counts = [len(gq) for gq in gauges]
+        g = np.concatenate([np.asarray(gq, dtype=np.int64) + self.cell_off[q] for q, gq in enumerate(gauges)])
+        g = np.ascontiguousarray(g, dtype=np.int64)
+        n_obs = n_steps // obs_every
+        traces = np.zeros((n_obs, len(g)))
+        self.batch._check(_lib.load().swe_batch_adjoint_forward(self.batch.b, int(scheme), int(n_steps),
+                                                                int(checkpoint_every), len(g), g.ctypes.data,
+                                                                int(obs_every), traces.ctypes.data))
+        cut = np.cumsum([0] + self.gauge_counts)
+        return [traces[:, cut[q]:cut[q + 1]] for q in range(len(self.meshes))]
+
+    def dts(self, n_steps: int) -> np.ndarray:
+        """(n_steps, n_instances) recorded dts."""
+        out = np.zeros((n_steps, len(self.meshes)))
+        self.batch._check(_lib.load().swe_batch_adjoint_dts(self.batch.b, out.ctypes.data))
+        return out
+
+    def backward(self, trace_grads):
+        """trace_grads: one array per instance, shaped like its traces.
+        Returns one (grad_prim0 (C_q, 3), grad_z (N_q,)) pair per instance."""
+        tg = np.ascontiguousarray(np.concatenate([np.asarray(t, dtype=np.float64) for t in trace_grads], axis=1))
+        gp = np.zeros((int(self.cell_off[-1]), 3))
+        gz = np.zeros(int(self.node_off[-1]))
+        self.batch._check(_lib.load().swe_batch_adjoint_backward(self.batch.b, tg.ctypes.data, gp.ctypes.data,
+                                                                 gz.ctypes.data))
+        return [(gp[self.cell_off[q]:self.cell_off[q + 1]], gz[self.node_off[q]:self.node_off[q + 1]])
+                for q in range(len(self.meshes))]
 
 
 def _torch_function():

@@ -558,7 +558,10 @@ swe_status swe_batch_run(swe_batch* b, int32_t scheme, double dt, int64_t n_step
   if (!b) return SWE_ERR_INVALID_ARGUMENT;
   if (scheme < 0 || scheme > 2 || n_steps < 0) return fail(&b->err, SWE_ERR_INVALID_ARGUMENT, "bad scheme or n_steps");
   if (!(dt > 0.) || !std::isfinite(dt)) return fail(&b->err, SWE_ERR_INVALID_ARGUMENT, "dt must be positive and finite");
-  cudaError_t e = cudaMemcpyAsync(b->eng.d_fixed_dt, &dt, sizeof(double), cudaMemcpyHostToDevice, b->eng.stream());
+  const std::vector<double> dts((size_t)b->eng.I(), dt);  // the same dt for every instance
+  cudaError_t e = cudaMemcpyAsync(b->eng.d_fixed_dt, dts.data(), dts.size() * sizeof(double), cudaMemcpyHostToDevice,
+                                  b->eng.stream());
+  if (e == cudaSuccess) e = cudaStreamSynchronize(b->eng.stream());
   if (e == cudaSuccess) e = b->eng.run_graph(scheme, 2, n_steps);
   if (e != cudaSuccess) return cuda_fail(&b->err, e, "swe_batch_run");
   return SWE_OK;
@@ -570,6 +573,45 @@ swe_status swe_batch_get_prim(swe_batch* b, int32_t q, double* prim_out) {
   const int64_t c0 = b->eng.cell_off[q], n = b->eng.cell_off[q + 1] - c0;
   return download_prim(b->eng, prim_out, c0, n, &b->err);
   SWE_GUARD_END(&b->err)
+}
+
+swe_status swe_batch_adjoint_forward(swe_batch* b, int32_t scheme, int64_t n_steps, int64_t checkpoint_every,
+                                     int32_t n_gauges, const int64_t* gauge_cells, int64_t obs_every,
+                                     double* traces_out) {
+  if (!b) return SWE_ERR_INVALID_ARGUMENT;
+  SWE_GUARD_BEGIN
+  if (scheme < 0 || scheme > 2 || n_steps <= 0 || checkpoint_every <= 0 || n_gauges < 0 || obs_every <= 0)
+    return fail(&b->err, SWE_ERR_INVALID_ARGUMENT, "bad scheme, step counts or gauge count");
+  if (n_gauges > 0 && (!gauge_cells || !traces_out))
+    return fail(&b->err, SWE_ERR_INVALID_ARGUMENT, "gauge_cells and traces_out are required");
+  std::vector<int> g(n_gauges);
+  for (int q = 0; q < n_gauges; ++q) {
+    if (gauge_cells[q] < 0 || gauge_cells[q] >= b->eng.C())
+      return fail(&b->err, SWE_ERR_INVALID_ARGUMENT, "gauge cell out of range");
+    g[q] = (int)gauge_cells[q];
+  }
+  std::string e = b->eng.adjoint_forward(scheme, n_steps, checkpoint_every, g.data(), n_gauges, obs_every,
+                                         traces_out);
+  if (!e.empty()) return fail(&b->err, SWE_ERR_CUDA, e);
+  return SWE_OK;
+  SWE_GUARD_END(&b->err)
+}
+
+swe_status swe_batch_adjoint_backward(swe_batch* b, const double* trace_grads, double* grad_prim0,
+                                      double* grad_bathymetry) {
+  if (!b || !grad_prim0 || !grad_bathymetry) return SWE_ERR_INVALID_ARGUMENT;
+  SWE_GUARD_BEGIN
+  std::string e = b->eng.adjoint_backward(trace_grads, grad_prim0, grad_bathymetry);
+  if (!e.empty()) return fail(&b->err, SWE_ERR_INVALID_ARGUMENT, e);
+  return SWE_OK;
+  SWE_GUARD_END(&b->err)
+}
+
+swe_status swe_batch_adjoint_dts(swe_batch* b, double* dts_out) {
+  if (!b || !dts_out) return SWE_ERR_INVALID_ARGUMENT;
+  std::string e = b->eng.adjoint_dts(dts_out);
+  if (!e.empty()) return fail(&b->err, SWE_ERR_INVALID_ARGUMENT, e);
+  return SWE_OK;
 }
 
 swe_status swe_batch_time(swe_batch* b, int32_t q, double* t) {

@@ -96,9 +96,11 @@ __global__ void k_seed_gauges_seg(double* lamw, const int* g, int n_g, const dou
   if (q < n_g) atomicAdd(lamw + g[q], tg[j * n_g + q]);
 }
 
-// *dst = dts[*s0 + loc]: the recorded dt of a step of the current segment
-__global__ void k_fetch_dt(double* dst, const double* dts, const long long* s0, long long loc) {
-  if (threadIdx.x == 0) *dst = dts[*s0 + loc];
+// dst[q] = dts[(*s0 + loc) I + q]: the recorded dts (one per instance) of a
+// step of the current segment
+__global__ void k_fetch_dt(double* dst, const double* dts, const long long* s0, long long loc, int n_inst) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < n_inst) dst[q] = dts[(*s0 + loc) * n_inst + q];
 }
 __global__ void k_set_i64(long long* dst, long long v) {
   if (threadIdx.x == 0) *dst = v;
@@ -894,7 +896,6 @@ void adjoint_state_delete(AdjointState* a) { delete a; }
 
 std::string Engine::adjoint_init() {
   if (adj_) return "";
-  if (I() != 1) return "the adjoint runs on a single-instance context";
   AdjointState* a = new AdjointState();
   const int64_t C = mesh_.C, E = mesh_.E, N = mesh_.N;
   AdjWork& w = a->aw;
@@ -912,31 +913,38 @@ std::string Engine::adjoint_init() {
   ok = ok && w.pwjac && w.padj;
   w.route = a->alloc<unsigned char>(3 * C);
   ok = ok && w.route;
-  // twin slots, node -> cells, edge nodes (host, from the instance's topology)
-  const HostInstance& h = host[0];
+  // twin slots, node -> cells, edge nodes over all instances (global ids:
+  // each instance's local index plus its offset)
   std::vector<int> twin(3 * C, -1), eown_k(E, -1), enb_k(E, -1), en(2 * E);
-  for (int64_t e = 0; e < E; ++e) {
-    en[2 * e] = (int)h.en[2 * e];
-    en[2 * e + 1] = (int)h.en[2 * e + 1];
-  }
-  for (int64_t i = 0; i < C; ++i)
-    for (int k = 0; k < 3; ++k) {
-      const int64_t e = h.ce[3 * i + k];
-      if (h.ec[2 * e] == i) eown_k[e] = (int)(k * C + i);
-      else enb_k[e] = (int)(k * C + i);
+  std::vector<int> ptr(N + 1, 0), cells(3 * C);
+  for (int q = 0; q < I(); ++q) {
+    const HostInstance& h = host[q];
+    const int64_t c0 = cell_off[q], e0 = edge_off[q], n0 = node_off[q];
+    for (int64_t e = 0; e < h.E; ++e) {
+      en[2 * (e0 + e)] = (int)(n0 + h.en[2 * e]);
+      en[2 * (e0 + e) + 1] = (int)(n0 + h.en[2 * e + 1]);
     }
+    for (int64_t i = 0; i < h.C; ++i)
+      for (int k = 0; k < 3; ++k) {
+        const int64_t e = h.ce[3 * i + k];
+        if (h.ec[2 * e] == i) eown_k[e0 + e] = (int)(k * C + c0 + i);
+        else enb_k[e0 + e] = (int)(k * C + c0 + i);
+        ptr[n0 + h.cn[3 * i + k] + 1]++;
+      }
+  }
   for (int64_t e = 0; e < E; ++e)
     if (eown_k[e] >= 0 && enb_k[e] >= 0) {
       twin[eown_k[e]] = enb_k[e];
       twin[enb_k[e]] = eown_k[e];
     }
-  std::vector<int> ptr(N + 1, 0), cells(3 * C);
-  for (int64_t i = 0; i < C; ++i)
-    for (int k = 0; k < 3; ++k) ptr[h.cn[3 * i + k] + 1]++;
   for (int64_t n = 0; n < N; ++n) ptr[n + 1] += ptr[n];
   std::vector<int> fill(ptr.begin(), ptr.end() - 1);
-  for (int64_t i = 0; i < C; ++i)
-    for (int k = 0; k < 3; ++k) cells[fill[h.cn[3 * i + k]]++] = (int)((i << 2) | k);
+  for (int q = 0; q < I(); ++q) {
+    const HostInstance& h = host[q];
+    const int64_t c0 = cell_off[q], n0 = node_off[q];
+    for (int64_t i = 0; i < h.C; ++i)
+      for (int k = 0; k < 3; ++k) cells[fill[n0 + h.cn[3 * i + k]]++] = (int)(((c0 + i) << 2) | k);
+  }
   int* d_twin = a->alloc<int>(3 * C);
   int* d_ptr = a->alloc<int>(N + 1);
   int* d_cells = a->alloc<int>(3 * C);
@@ -983,7 +991,8 @@ std::string Engine::adjoint_forward(int scheme, int64_t n_steps, int64_t ckpt, c
   a.obs = obs;
   a.n_gauges = n_gauges;
   const int64_t n_obs = obs > 0 ? n_steps / obs : 0;
-  if (cudaMalloc(&a.d_dt, (n_steps ? n_steps : 1) * sizeof(double)) != cudaSuccess) return "tape allocation failed";
+  const int64_t NI = I();
+  if (cudaMalloc(&a.d_dt, (n_steps ? n_steps : 1) * NI * sizeof(double)) != cudaSuccess) return "tape allocation failed";
   if (cudaMalloc(&a.d_traces, (n_obs * n_gauges ? n_obs * n_gauges : 1) * sizeof(double)) != cudaSuccess)
     return "tape allocation failed";
   if (cudaMalloc(&a.d_gauges, (n_gauges ? n_gauges : 1) * sizeof(int)) != cudaSuccess) return "tape allocation failed";
@@ -1004,7 +1013,7 @@ std::string Engine::adjoint_forward(int scheme, int64_t n_steps, int64_t ckpt, c
     // the plain step's CUDA graph (dt = CFLdt() of the previous flux pass)
     cudaError_t e = run_graph(scheme, 1, 1);
     if (e != cudaSuccess) return std::string("forward step: ") + cudaGetErrorString(e);
-    cudaMemcpyAsync(a.d_dt + n, work_.dt, sizeof(double), cudaMemcpyDeviceToDevice, stream_);
+    cudaMemcpyAsync(a.d_dt + n * NI, work_.dt, NI * sizeof(double), cudaMemcpyDeviceToDevice, stream_);
     if (obs > 0 && (n + 1) % obs == 0 && n_gauges > 0) {
       const int64_t j = (n + 1) / obs - 1;
       k_gather_gauges<<<(n_gauges + 255) / 256, 256, 0, stream_>>>(state(0, 0), a.d_gauges, n_gauges,
@@ -1022,7 +1031,7 @@ std::string Engine::adjoint_forward(int scheme, int64_t n_steps, int64_t ckpt, c
 
 std::string Engine::adjoint_dts(double* out_host) {
   if (!adj_ || !adj_->taped) return "no taped forward run";
-  cudaError_t e = cudaMemcpy(out_host, adj_->d_dt, adj_->n_steps * sizeof(double), cudaMemcpyDeviceToHost);
+  cudaError_t e = cudaMemcpy(out_host, adj_->d_dt, adj_->n_steps * I() * sizeof(double), cudaMemcpyDeviceToHost);
   return e == cudaSuccess ? "" : cudaGetErrorString(e);
 }
 
@@ -1108,8 +1117,8 @@ std::string Engine::adjoint_backward(const double* trace_grads_host, double* gra
   cudaMemsetAsync(w.lam, 0, 3 * C * sizeof(double), stream_);
   cudaMemsetAsync(w.lz, 0, N * sizeof(double), stream_);
   cudaMemsetAsync(w.lscatter, 0, C * sizeof(double), stream_);
-  double tsum_saved = 0.;  // the recompute must not advance the context's clock
-  cudaMemcpyAsync(&tsum_saved, work_.tsum, sizeof(double), cudaMemcpyDeviceToHost, stream_);
+  std::vector<double> tsum_saved((size_t)I(), 0.);  // the recompute must not advance the clocks
+  cudaMemcpyAsync(tsum_saved.data(), work_.tsum, I() * sizeof(double), cudaMemcpyDeviceToHost, stream_);
   cudaStreamSynchronize(stream_);
   double* lam_step = nullptr;  // adjoint of the current step's end state
   cudaMalloc(&lam_step, 3 * C * sizeof(double));
@@ -1127,7 +1136,7 @@ std::string Engine::adjoint_backward(const double* trace_grads_host, double* gra
   auto enqueue_recompute = [&](int64_t len) -> cudaError_t {
     for (int64_t loc = 0; loc < len; ++loc) {
       const int64_t base = loc * ns;
-      k_fetch_dt<<<1, 32, 0, stream_>>>(d_fixed_dt, a.d_dt, d_s0, loc);
+      k_fetch_dt<<<(I() + 127) / 128, 128, 0, stream_>>>(d_fixed_dt, a.d_dt, d_s0, loc, I());
       double* S0p = store[base];
       const double* u0[3] = {S0p, S0p + C, S0p + 2 * C};
       for (int s = 0; s < ns; ++s) {
@@ -1174,7 +1183,7 @@ std::string Engine::adjoint_backward(const double* trace_grads_host, double* gra
       if (seeds)
         k_seed_gauges_seg<<<(a.n_gauges + 255) / 256, 256, 0, stream_>>>(lam_step, a.d_gauges, a.n_gauges, d_tg,
                                                                          d_s0, loc, a.obs);
-      k_fetch_dt<<<1, 32, 0, stream_>>>(work_.dt, a.d_dt, d_s0, loc);
+      k_fetch_dt<<<(I() + 127) / 128, 128, 0, stream_>>>(work_.dt, a.d_dt, d_s0, loc, I());
       double* S0p = store[base];
       const double* u0[3] = {S0p, S0p + C, S0p + 2 * C};
       cudaMemsetAsync(w.lam0, 0, 3 * C * sizeof(double), stream_);
@@ -1245,7 +1254,7 @@ std::string Engine::adjoint_backward(const double* trace_grads_host, double* gra
     cudaError_t e = cudaStreamSynchronize(stream_);
     if (e != cudaSuccess) err = std::string("adjoint: ") + cudaGetErrorString(e);
   }
-  cudaMemcpy(work_.tsum, &tsum_saved, sizeof(double), cudaMemcpyHostToDevice);
+  cudaMemcpy(work_.tsum, tsum_saved.data(), I() * sizeof(double), cudaMemcpyHostToDevice);
   if (kept_pool) cudaFree(kept_pool);
   for (auto& p : store) cudaFree(p);
   cudaFree(d_tg);

@@ -102,7 +102,7 @@ struct DevWork {
   unsigned long long* r;       // [I] ordered key of min length-to-wavespeed
   double* dt;                  // [I] step dt
   double* tsum;                // [I] accumulated time
-  const double* fixed_dt;      // [1] dt for fixed-step runs
+  const double* fixed_dt;      // [I] dt for fixed-step runs
   unsigned* err;               // [1] error bits
 };
 
@@ -199,7 +199,7 @@ class Engine {
   std::vector<HostInstance> host;
   double* d_io = nullptr;        // [3C] staging buffer for the interleaved 3 x C field
   unsigned* d_ioflag = nullptr;  // non-finite flag of the last upload
-  double* d_fixed_dt = nullptr;  // device scalar
+  double* d_fixed_dt = nullptr;  // [I] device dt of fixed-step runs
   double* h_fixed_dt = nullptr;  // pinned host scalar
 
  private:

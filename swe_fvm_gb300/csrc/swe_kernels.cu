@@ -131,7 +131,7 @@ __global__ void __launch_bounds__(256) k_recon1(DevMesh m, DevWork wk, const dou
         wk.dt[inst] = dt;
         wk.tsum[inst] += dt;
       } else if (latch_mode == 2) {
-        double dt = *wk.fixed_dt;
+        double dt = wk.fixed_dt[BATCH ? inst : 0];
         wk.dt[inst] = dt;
         wk.tsum[inst] += dt;
       }
@@ -656,7 +656,7 @@ std::string Engine::init(std::vector<HostInstance>&& inst, int flux, int ws, int
   Wk.r = dalloc<unsigned long long>(I);
   Wk.dt = dalloc<double>(I);
   Wk.tsum = dalloc<double>(I);
-  d_fixed_dt = dalloc<double>(1);
+  d_fixed_dt = dalloc<double>(I);  // per instance
   Wk.fixed_dt = d_fixed_dt;
   Wk.err = dalloc<unsigned>(1);
   for (int q = 0; q < 6; ++q) state_[q] = dalloc<double>(C);
