@@ -267,6 +267,8 @@ def run_gpu(args):
         out["batched"] = run_ensemble(torch, stream)
     if ADJ_STEPS > 0 and not args.no_adjoint:
         out["adjoint"] = run_adjoint(torch, stream)
+    if BADJ_INSTANCES > 0 and not args.no_batch_adjoint:
+        out["batched_adjoint"] = run_batch_adjoint(torch, stream)
     if rank == 0:
         if world == 1 and not args.no_cpu:
             out["cpu_baseline"] = cpu_baseline(mesh, prim)
@@ -396,6 +398,68 @@ def run_adjoint(torch, stream):
             "config": {"workload": "adjoint_250k", "flux": "HLLC+Einfeldt", "scheme": "SSPRK2", "cfl": 0.15}}
 
 
+BADJ_INSTANCES = int(os.environ.get("SWE_BENCH_BADJ_INSTANCES", "64"))
+BADJ_STEPS = int(os.environ.get("SWE_BENCH_BADJ_STEPS", "500"))
+
+
+def run_batch_adjoint(torch, stream):
+    """Batched-adjoint config: 64 seeded instances of 20k-100k cells (the
+    ensemble's generator), HLLC + Einfeldt, SSPRK2, per-instance CFL 0.4, 500
+    steps, 16 random gauge cells per instance observed every 10th step,
+    checkpoint every 25 steps; targets from runs whose bathymetry carries 5%
+    seeded Gaussian noise.  Reports (taped forward + backward) / plain batched
+    forward, all instances in single launches."""
+    from swe_fvm_gb300 import Batch, Fluxes, Wavespeeds, scenarios
+    from swe_fvm_gb300.adjoint import BatchRollout
+    from swe_fvm_gb300.mesh import Mesh
+
+    t0 = time.time()
+    ens = scenarios.adjoint_ensemble(BADJ_INSTANCES)
+    t_gen = time.time() - t0
+    meshes = [m.contiguous() for m, _ in ens]
+    prims = [p for _, p in ens]
+    cells = sum(m.num_cells for m in meshes)
+    rng = np.random.default_rng(13)
+    gauges = [rng.choice(m.num_cells, 16, replace=False) for m in meshes]
+    obs, ckpt = 10, 25
+    noisy = []
+    for m in meshes:
+        g = m.geometry.copy()
+        g[:, 2] = g[:, 2] * (1.0 + 0.05 * rng.standard_normal(m.num_nodes))
+        noisy.append(Mesh(g, m.edge_nodes, m.edge_cells, m.cell_nodes, m.cell_edges, m.cell_neighbours))
+    targets = BatchRollout(noisy, prims, cfl=0.4).forward(1, BADJ_STEPS, ckpt, gauges, obs)
+    # plain batched forward
+    b = Batch(meshes, prims, Fluxes.HLLC(Wavespeeds.Einfeldt), cfl=0.4)
+    b.set_stream(stream.cuda_stream)
+    b.run_cfl(1, 2)  # graph capture outside the timed region
+    b.synchronize()
+    del b
+    b = Batch(meshes, prims, Fluxes.HLLC(Wavespeeds.Einfeldt), cfl=0.4)
+    b.set_stream(stream.cuda_stream)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    b.run_cfl(1, BADJ_STEPS)
+    b.synchronize()
+    t_plain = time.perf_counter() - t0
+    del b
+    br = BatchRollout(meshes, prims, cfl=0.4)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    traces = br.forward(1, BADJ_STEPS, ckpt, gauges, obs)
+    t_fwd = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    grads = br.backward([2.0 * (t - tg) for t, tg in zip(traces, targets)])
+    t_bwd = time.perf_counter() - t0
+    loss = float(sum(np.sum((t - tg) ** 2) for t, tg in zip(traces, targets)))
+    return {"metric": "batched adjoint/forward time ratio (taped forward + backward) / plain batched forward",
+            "ratio": (t_fwd + t_bwd) / t_plain, "higher_is_better": False, "plain_forward_s": t_plain,
+            "taped_forward_s": t_fwd, "backward_s": t_bwd, "instances": len(meshes), "cells": cells,
+            "steps": BADJ_STEPS, "gauges_per_instance": 16, "obs_every": obs, "checkpoint_every": ckpt,
+            "loss": loss, "grad_norm_z": float(np.sqrt(sum(np.sum(gz ** 2) for _, gz in grads))),
+            "config": {"workload": "batched_adjoint_64", "cells_per_instance": "uniform 20k-100k",
+                       "flux": "HLLC+Einfeldt", "scheme": "SSPRK2", "cfl": 0.4, "mesh_gen_s": round(t_gen, 1)}}
+
+
 # DRAM bytes per SSPRK2 step (dram__bytes_read.sum + dram__bytes_write.sum over
 # the step's 12 kernels, one ncu launch capture of the 1M-cell mesh, lattice
 # 708, the same command line with --profile).
@@ -450,6 +514,7 @@ def main():
     ap.add_argument("--no-ensemble", action="store_true", help="skip the batched-ensemble leg")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint leg")
     ap.add_argument("--adjoint-profile", action="store_true", help="only a short taped run and its reverse")
+    ap.add_argument("--no-batch-adjoint", action="store_true", help="skip the batched-adjoint leg")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

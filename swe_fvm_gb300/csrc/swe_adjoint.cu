@@ -678,6 +678,15 @@ __device__ void pw_jacobian(const DevMesh& m, const DevWork& wk, const AdjWork& 
                                   F4::var(m.zn[2 * C + best], 3), pc.w0);
           J.route = 3;
           for (int q = 0; q < 4; ++q) J.rc[q] = y.d[q];
+          // Regularised at the wetting front: the level is b23 + cbrt(3 h K)
+          // for small depth h, whose slope in w grows like h^(-2/3); fed back
+          // through PartWet2 it made the reverse grow geometrically (1e24
+          // after 500 steps on beds whose bumps emerge) while finite
+          // differences of the forward stay ~1e-5.  Below the reference's
+          // desingularisation depth kEta1 the w-slope is taken at h = kEta1
+          // (scaled by (h / kEta1)^(2/3)).
+          const double hb = W[best] - m.bc[best];
+          if (dltc(hb, kEta1)) J.rc[0] *= dge0(hb) ? cbrt(SWE_DIV(hb * hb, kEta1 * kEta1)) : 0.;
         }
       }
     }

@@ -189,6 +189,23 @@ def ensemble(n_instances: int = 256, lo: int = 2000, hi: int = 200000, seed0: in
         return pool.map(_hump_job, jobs, chunksize=1)
 
 
+def adjoint_ensemble(n_instances: int = 64, lo: int = 20000, hi: int = 100000, seed0: int = 5000,
+                     processes: int = 0):
+    """Batched-adjoint config: n_instances seeded instances (the ensemble's
+    generator, instance i with seed seed0 + i) with cell counts uniform in
+    [lo, hi]."""
+    import multiprocessing as mp
+    import os
+
+    sizes = np.random.default_rng(seed0).uniform(lo, hi, n_instances)
+    jobs = [(seed0 + i, int(c)) for i, c in enumerate(sizes)]
+    nproc = processes or max(1, min(16, (os.cpu_count() or 1)))
+    if nproc == 1:
+        return [_hump_job(j) for j in jobs]
+    with mp.get_context("spawn").Pool(nproc) as pool:
+        return pool.map(_hump_job, jobs, chunksize=1)
+
+
 # ---------------------------------------------------------------- small cases
 def lake_at_rest(n: int = 32, level: float = 0.0):
     """Still water over a stepped bed on [0,4]^2 (examples/Tests.h:37-42): bed
