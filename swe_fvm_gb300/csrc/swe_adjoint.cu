@@ -327,7 +327,7 @@ __global__ void __launch_bounds__(256) k_adj_flux(DevMesh m, DevWork wk, AdjWork
   SideState L{wk.ew[sl], wk.eu[sl], wk.ev[sl]};
   SideState R{wk.ew[sr], wk.eu[sr], wk.ev[sr]};
   double lL[3] = {0., 0., 0.}, lR[3] = {0., 0., 0.}, lb = 0.;
-  flux_reverse(FLUX, WS, g, L, R, lF, lL, lR, &lb);
+  flux_reverse(FLUX, WS, g, L, R, lF, lL, lR, &lb, wk.ftape, m.E, e);
   aw.lew[sl] += lL[0];
   aw.leu[sl] += lL[1];
   aw.lev[sl] += lL[2];
@@ -1080,7 +1080,7 @@ std::string Engine::adjoint_backward(const double* trace_grads_host, double* gra
   // per-stage forward intermediates of one segment (interface slots, fluxes,
   // draining dt, node maxima, part-wet list) when device memory allows
   const int64_t E = mesh_.E;
-  const size_t per_stage = ((15 * C + 3 * E + 5 * C) * sizeof(double) + N * sizeof(unsigned long long) +
+  const size_t per_stage = ((15 * C + 10 * E + 5 * C) * sizeof(double) + N * sizeof(unsigned long long) +
                             (C + 1) * sizeof(int) + C + 255) / 256 * 256;
   size_t free_b = 0, total_b = 0;
   cudaMemGetInfo(&free_b, &total_b);
@@ -1112,6 +1112,7 @@ std::string Engine::adjoint_backward(const double* trace_grads_host, double* gra
       wq.f0 = (double*)take(E * sizeof(double));
       wq.f1 = (double*)take(E * sizeof(double));
       wq.f2 = (double*)take(E * sizeof(double));
+      wq.ftape = (double*)take(7 * E * sizeof(double));
       wq.drain = (double*)take(C * sizeof(double));
       wq.pwrec = (double*)take(C * sizeof(double));
       wq.maxwp = (unsigned long long*)take(N * sizeof(unsigned long long));

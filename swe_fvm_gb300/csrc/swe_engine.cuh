@@ -99,6 +99,7 @@ struct DevWork {
   // [C] pass-1 class of each cell: type (0 dry, 1 partially wet, 2 fully wet)
   // | neighbour combination mask << 2 | combination plane kept << 5
   unsigned char* cls;
+  double* ftape;               // [7][E] flux intermediates kept for the adjoint, or null
   unsigned long long* r;       // [I] ordered key of min length-to-wavespeed
   double* dt;                  // [I] step dt
   double* tsum;                // [I] accumulated time

@@ -138,9 +138,12 @@ SWE_HD void wavespeeds_rev(int ws, const WsFwd& f, double ul, double ur, double 
 
 // Reverse of one interior edge's flux.  g: edge geometry; L, R: interface
 // primitives; lF: adjoint of (F0, F1, F2).  Adds to lL[3], lR[3] (w, u, v)
-// and *lb (edge bathymetry).
+// and *lb (edge bathymetry).  tape: null, or the forward's stored wave-speed
+// intermediates and u* of this edge (EdgeTape layout, tape[k E + e]), which
+// then are not recomputed.
 SWE_HD void flux_reverse(int flux, int ws, const EdgeGeom& g, const SideState& L, const SideState& R,
-                         const double* lF, double* lL, double* lR, double* lb) {
+                         const double* lF, double* lL, double* lR, double* lb, const double* tape = nullptr,
+                         int E = 0, int e = 0) {
   const double nx = g.nx, ny = g.ny, tx = g.tx, ty = g.ty;
   const double ul = L.u * nx + L.v * ny;
   const double hl = L.w - g.b;
@@ -149,7 +152,18 @@ SWE_HD void flux_reverse(int flux, int ws, const EdgeGeom& g, const SideState& L
   if (!dgtc(hl + hr, kMinCapture)) return;
   double lul = 0., lhl = 0., lur = 0., lhr = 0., lvl = 0., lvr = 0.;
   double lLu = 0., lLv = 0., lRu = 0., lRv = 0.;
-  const WsFwd f = ws_forward(ws, ul, hl, ur, hr);
+  WsFwd f;
+  if (tape) {
+    f.cl = tape[e];
+    f.cr = tape[E + e];
+    f.S = f.cl + f.cr;
+    f.uRoe = tape[2 * E + e];
+    f.cRoe = tape[3 * E + e];
+    f.a0 = tape[4 * E + e];
+    f.a1 = tape[5 * E + e];
+  } else {
+    f = ws_forward(ws, ul, hl, ur, hr);
+  }
   if (flux == 0) {
     const double a0 = f.a0, a1 = f.a1;
     const double al = smin(0., a0);
@@ -198,10 +212,10 @@ SWE_HD void flux_reverse(int flux, int ws, const EdgeGeom& g, const SideState& L
   } else {
     const double al = f.a0, ar = f.a1;
     const double A = ar - ur, B = al - ul;
-    // u* with the forward's operations (its sign picks the star side)
-    const double N = A * hr * ur - B * hl * ul + 0.5 * (hl * hl - hr * hr);
+    // u* with the forward's operations (its sign picks the star side), or the
+    // forward's own value
     const double D = hr * A - hl * B;
-    const double us = SWE_DIV(N, D);
+    const double us = tape ? tape[6 * E + e] : SWE_DIV(A * hr * ur - B * hl * ul + 0.5 * (hl * hl - hr * hr), D);
     double lus = 0., lA = 0., lB = 0., lar = 0., lal = 0.;
     if (!dgt0(us)) {
       const double vr = fma(R.u, tx, R.v * ty);

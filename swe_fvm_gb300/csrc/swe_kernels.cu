@@ -322,7 +322,7 @@ __global__ void __launch_bounds__(256) k_recon2(DevMesh m, DevWork wk, const dou
 // SpaceDisc::ComputeFluxes with flux plugin FLUX and the CFL min-reduction.
 // The flux of edge e (src/SpaceDisc.cpp:54-74) into f0..f2; *lw receives its
 // length-to-wavespeed ratio or stays +inf.
-template <class FLUX>
+template <class FLUX, bool TAPE>
 __device__ __forceinline__ void flux_edge(const DevMesh& m, const DevWork& wk, const double* __restrict__ W, int e,
                                           int inst, double* lw) {
   const int o = m.eown[e];
@@ -341,7 +341,8 @@ __device__ __forceinline__ void flux_edge(const DevMesh& m, const DevWork& wk, c
     const int sl = m.eslotl[e], sr = m.eslotr[e];
     SideState L{wk.ew[sl], wk.eu[sl], wk.ev[sl]};
     SideState R{wk.ew[sr], wk.eu[sr], wk.ev[sr]};
-    FLUX::eval(g, L, R, m.inst_cor[inst], lw, F);
+    if (TAPE) FLUX::eval(g, L, R, m.inst_cor[inst], lw, F, EdgeTape{wk.ftape, m.E, e});
+    else FLUX::eval(g, L, R, m.inst_cor[inst], lw, F);
   }
   wk.f0[e] = F[0];
   wk.f1[e] = F[1];
@@ -350,7 +351,8 @@ __device__ __forceinline__ void flux_edge(const DevMesh& m, const DevWork& wk, c
 
 // MODE 0: every edge.  MODE 1: the edges none of whose cells is partially
 // wet (the others wait for PartWet2 and go through k_flux_pw).
-template <class FLUX, bool BATCH, int MODE>
+// TAPE: also store the intermediates the adjoint's reverse reads (wk.ftape).
+template <class FLUX, bool BATCH, int MODE, bool TAPE>
 __global__ void __launch_bounds__(256) k_flux(DevMesh m, DevWork wk, const double* __restrict__ W) {
   __shared__ unsigned long long s_min[32];
   __shared__ int s_inst[32];
@@ -364,7 +366,7 @@ __global__ void __launch_bounds__(256) k_flux(DevMesh m, DevWork wk, const doubl
       const int nb = m.enb[e];
       mine = !(((wk.cls[m.eown[e]] & 3) == 1) || (nb >= 0 && (wk.cls[nb] & 3) == 1));
     }
-    if (mine) flux_edge<FLUX>(m, wk, W, e, inst, &lw);
+    if (mine) flux_edge<FLUX, TAPE>(m, wk, W, e, inst, &lw);
   }
   // min-reduction of the length-to-wavespeed ratio on order-preserving integer
   // keys (exact): warp, block, one atomicMin per block and instance
@@ -413,7 +415,7 @@ __global__ void __launch_bounds__(256) k_flux(DevMesh m, DevWork wk, const doubl
 // The fluxes of the edges next to the stage's partially-wet cells (after
 // PartWet2): listed cell i takes its local edge k unless the edge's owner is
 // partially wet too and is not i, so that each edge is evaluated once.
-template <class FLUX, bool BATCH>
+template <class FLUX, bool BATCH, bool TAPE>
 __global__ void __launch_bounds__(128) k_flux_pw(DevMesh m, DevWork wk, const double* __restrict__ W) {
   const int C = m.C;
   const int n = 3 * min(*wk.pwcount, C);
@@ -425,7 +427,7 @@ __global__ void __launch_bounds__(128) k_flux_pw(DevMesh m, DevWork wk, const do
     if ((((wk.cls[o] & 3) == 1) ? o : m.enb[e]) != i) continue;
     const int inst = BATCH ? m.einst[e] : 0;
     double lw = kInf;
-    flux_edge<FLUX>(m, wk, W, e, inst, &lw);
+    flux_edge<FLUX, TAPE>(m, wk, W, e, inst, &lw);
     if (dbits(lw) != dbits(kInf)) atomicMin(wk.r + inst, order_key(lw));
   }
 }
@@ -653,6 +655,7 @@ std::string Engine::init(std::vector<HostInstance>&& inst, int flux, int ws, int
   Wk.pwcount = dalloc<int>(1);
   Wk.pwrec = dalloc<double>(C);
   Wk.cls = dalloc<unsigned char>(C);
+  Wk.ftape = nullptr;
   Wk.r = dalloc<unsigned long long>(I);
   Wk.dt = dalloc<double>(I);
   Wk.tsum = dalloc<double>(I);
@@ -742,22 +745,33 @@ cudaError_t Engine::interface_values(const double* W, const double* U, const dou
   return cudaGetLastError();
 }
 
+template <class FLUX, bool TAPE>
+static void launch_flux_t(bool batched, int mode, int blocks, int b, cudaStream_t s, const DevMesh& m,
+                          const DevWork& w, const double* W) {
+  if (batched) {
+    if (mode) k_flux<FLUX, true, 1, TAPE><<<blocks, b, 0, s>>>(m, w, W);
+    else k_flux<FLUX, true, 0, TAPE><<<blocks, b, 0, s>>>(m, w, W);
+  } else {
+    if (mode) k_flux<FLUX, false, 1, TAPE><<<blocks, b, 0, s>>>(m, w, W);
+    else k_flux<FLUX, false, 0, TAPE><<<blocks, b, 0, s>>>(m, w, W);
+  }
+}
 template <class FLUX>
 static void launch_flux(bool batched, int mode, int blocks, int b, cudaStream_t s, const DevMesh& m,
                         const DevWork& w, const double* W) {
-  if (batched) {
-    if (mode) k_flux<FLUX, true, 1><<<blocks, b, 0, s>>>(m, w, W);
-    else k_flux<FLUX, true, 0><<<blocks, b, 0, s>>>(m, w, W);
-  } else {
-    if (mode) k_flux<FLUX, false, 1><<<blocks, b, 0, s>>>(m, w, W);
-    else k_flux<FLUX, false, 0><<<blocks, b, 0, s>>>(m, w, W);
-  }
+  if (w.ftape) launch_flux_t<FLUX, true>(batched, mode, blocks, b, s, m, w, W);
+  else launch_flux_t<FLUX, false>(batched, mode, blocks, b, s, m, w, W);
 }
 template <class FLUX>
 static void launch_flux_pw(bool batched, int blocks, cudaStream_t s, const DevMesh& m, const DevWork& w,
                            const double* W) {
-  if (batched) k_flux_pw<FLUX, true><<<blocks, 128, 0, s>>>(m, w, W);
-  else k_flux_pw<FLUX, false><<<blocks, 128, 0, s>>>(m, w, W);
+  if (w.ftape) {
+    if (batched) k_flux_pw<FLUX, true, true><<<blocks, 128, 0, s>>>(m, w, W);
+    else k_flux_pw<FLUX, false, true><<<blocks, 128, 0, s>>>(m, w, W);
+  } else {
+    if (batched) k_flux_pw<FLUX, true, false><<<blocks, 128, 0, s>>>(m, w, W);
+    else k_flux_pw<FLUX, false, false><<<blocks, 128, 0, s>>>(m, w, W);
+  }
 }
 
 cudaError_t Engine::fluxes(const double* W) { return fluxes(W, 0); }

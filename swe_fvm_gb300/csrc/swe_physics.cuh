@@ -257,31 +257,68 @@ SWE_HD void elem_flux(double nx, double ny, double h, double hu, double hv, doub
 
 // Wave-speed plugins (src/Fluxes.cpp:5-26).  speeds() returns the pair the
 // reference's Array<2> holds.
+// What a flux evaluation can leave for its reverse: the wave speeds'
+// intermediates and u* (the discrete adjoint's recompute stores them, see
+// swe_flux_adjoint.cuh).  NoTape records nothing and compiles away.
+struct NoTape {
+  SWE_HD void speeds(double, double, double, double, double, double) const {}
+  SWE_HD void ustar(double) const {}
+};
+// Edge e's intermediates into t[k * E + e]: cl, cr, uRoe, cRoe, a0, a1, u*.
+struct EdgeTape {
+  double* t;
+  int E, e;
+  SWE_HD void speeds(double cl, double cr, double uRoe, double cRoe, double a0, double a1) const {
+    t[e] = cl;
+    t[E + e] = cr;
+    t[2 * E + e] = uRoe;
+    t[3 * E + e] = cRoe;
+    t[4 * E + e] = a0;
+    t[5 * E + e] = a1;
+  }
+  SWE_HD void ustar(double us) const { t[6 * E + e] = us; }
+};
+
 struct Rusanov {
   static constexpr int id = 0;
-  SWE_HD static void speeds(double ul, double hl, double ur, double hr, double* a0, double* a1) {
+  template <class T>
+  SWE_HD static void speeds(double ul, double hl, double ur, double hr, double* a0, double* a1, const T& tape) {
     double cl = SWE_SQRT(hl), cr = SWE_SQRT(hr);
     double ap = smax(fabs(ul) + cl, fabs(ur) + cr);
     *a0 = -ap;
     *a1 = ap;
+    tape.speeds(cl, cr, 0., 0., *a0, *a1);
+  }
+  SWE_HD static void speeds(double ul, double hl, double ur, double hr, double* a0, double* a1) {
+    speeds(ul, hl, ur, hr, a0, a1, NoTape{});
   }
 };
 struct Davis {
   static constexpr int id = 1;
-  SWE_HD static void speeds(double ul, double hl, double ur, double hr, double* a0, double* a1) {
+  template <class T>
+  SWE_HD static void speeds(double ul, double hl, double ur, double hr, double* a0, double* a1, const T& tape) {
     double cl = SWE_SQRT(hl), cr = SWE_SQRT(hr);
     *a0 = smin(ul - cl, ur - cr);
     *a1 = smax(ul + cl, ur + cr);
+    tape.speeds(cl, cr, 0., 0., *a0, *a1);
+  }
+  SWE_HD static void speeds(double ul, double hl, double ur, double hr, double* a0, double* a1) {
+    speeds(ul, hl, ur, hr, a0, a1, NoTape{});
   }
 };
 struct Einfeldt {
   static constexpr int id = 2;
-  SWE_HD static void speeds(double ul, double hl, double ur, double hr, double* a0, double* a1) {
+  template <class T>
+  SWE_HD static void speeds(double ul, double hl, double ur, double hr, double* a0, double* a1, const T& tape) {
     double cl = SWE_SQRT(hl), cr = SWE_SQRT(hr);
     double uRoe = SWE_DIV(cl * ul + cl * ur, cl + cr);  // the reference's cl * ur
     double cRoe = SWE_SQRT(SWE_HALF(hl + hr));
     *a0 = smin(ul - cl, uRoe - cRoe);
     *a1 = smax(ur + cr, uRoe + cRoe);
+    tape.speeds(cl, cr, uRoe, cRoe, *a0, *a1);
+  }
+  SWE_HD static void speeds(double ul, double hl, double ur, double hr, double* a0, double* a1) {
+    speeds(ul, hl, ur, hr, a0, a1, NoTape{});
   }
 };
 
@@ -305,6 +342,11 @@ struct HLL {
   static constexpr int id = 0;
   SWE_HD static void eval(const EdgeGeom& g, const SideState& L, const SideState& R, double cor, double* lw,
                           double* F) {
+    eval(g, L, R, cor, lw, F, NoTape{});
+  }
+  template <class T>
+  SWE_HD static void eval(const EdgeGeom& g, const SideState& L, const SideState& R, double cor, double* lw,
+                          double* F, const T& tape) {
     double ul = L.u * g.nx + L.v * g.ny;
     double hl = L.w - g.b;
     double ur = R.u * g.nx + R.v * g.ny;
@@ -312,7 +354,7 @@ struct HLL {
     F[0] = 0.; F[1] = 0.; F[2] = 0.;
     if (!dgtc(hl + hr, kMinCapture)) return;
     double a0, a1;
-    W::speeds(ul, hl, ur, hr, &a0, &a1);
+    W::speeds(ul, hl, ur, hr, &a0, &a1, tape);
     double al = smin(0., a0);
     double ar = smax(0., a1);
     if (!dgtc(ar - al, kMinCapture)) return;
@@ -333,6 +375,11 @@ struct HLLC {
   static constexpr int id = 1;
   SWE_HD static void eval(const EdgeGeom& g, const SideState& L, const SideState& R, double cor, double* lw,
                           double* F) {
+    eval(g, L, R, cor, lw, F, NoTape{});
+  }
+  template <class T>
+  SWE_HD static void eval(const EdgeGeom& g, const SideState& L, const SideState& R, double cor, double* lw,
+                          double* F, const T& tape) {
     double ul = L.u * g.nx + L.v * g.ny;
     double hl = L.w - g.b;
     double ur = R.u * g.nx + R.v * g.ny;
@@ -340,12 +387,13 @@ struct HLLC {
     F[0] = 0.; F[1] = 0.; F[2] = 0.;
     if (!dgtc(hl + hr, kMinCapture)) return;
     double al, ar;
-    W::speeds(ul, hl, ur, hr, &al, &ar);
+    W::speeds(ul, hl, ur, hr, &al, &ar, tape);
     // (ar - ur) hr = hr (ar - ur) and (al - ul) hl = hl (al - ul) bit for bit:
     // each product is formed once for u* and the star depth
     const double hrA = (ar - ur) * hr, hlB = (al - ul) * hl;
     double ustar = hrA * ur - hlB * ul + SWE_HALF(hl * hl - hr * hr);
     ustar = SWE_DIV(ustar, hrA - hlB);
+    tape.ustar(ustar);
     *lw = SWE_DIV(g.lmin, fabs(cor) + smax(kTol, smax(al, ar)));
     // u* <= 0: the right star state, else the left one.  The side is picked
     // first and the shared formula evaluated once, so a warp whose edges take
