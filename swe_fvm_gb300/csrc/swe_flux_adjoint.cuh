@@ -217,68 +217,54 @@ SWE_HD void flux_reverse(int flux, int ws, const EdgeGeom& g, const SideState& L
     const double D = hr * A - hl * B;
     const double us = tape ? tape[6 * E + e] : SWE_DIV(A * hr * ur - B * hl * ul + 0.5 * (hl * hl - hr * hr), D);
     double lus = 0., lA = 0., lB = 0., lar = 0., lal = 0.;
-    if (!dgt0(us)) {
-      const double vr = fma(R.u, tx, R.v * ty);
-      const double ihr = is_wet(hr) ? SWE_DIV(1., hr) : 0.;
-      const double Ur[3] = {hr, hr * R.u, hr * R.v};
-      const double uxs = fma(vr, tx, us * ty);
-      const double vys = fma(vr, nx, us * ny);
-      const double iY = SWE_DIV(1., ar - us);
-      const double hs = hr * A * iY;
-      const double Us[3] = {hs, hs * uxs, hs * vys};
-      const double sp = smax(0., ar);
-      double lsp = 0., lUr[3], lUs[3];
+    // the star side the forward took (u* <= 0: right), evaluated once and
+    // scattered by selects, so a warp whose edges take both sides issues it once
+    const bool right = !dgt0(us);
+    const SideState& X = right ? R : L;
+    const double hx = right ? hr : hl, Kx = right ? A : B, ax = right ? ar : al;
+    const double vtx = fma(X.u, tx, X.v * ty);
+    const double ihx = is_wet(hx) ? SWE_DIV(1., hx) : 0.;
+    const double Ux[3] = {hx, hx * X.u, hx * X.v};
+    const double uxs = fma(vtx, tx, us * ty);
+    const double vys = fma(vtx, nx, us * ny);
+    const double iY = SWE_DIV(1., ax - us);
+    const double hs = hx * Kx * iY;
+    const double Us[3] = {hs, hs * uxs, hs * vys};
+    const double sx = right ? smax(0., ar) : smin(0., al);
+    double lsx = 0., lUx[3], lUs[3];
 #pragma unroll
-      for (int q = 0; q < 3; ++q) {
-        lsp = fma(lF[q], Us[q] - Ur[q], lsp);
-        lUs[q] = sp * lF[q];
-        lUr[q] = -lUs[q];
-      }
-      if (dlt(0., ar)) lar += lsp;
-      elem_flux_rev(nx, ny, Ur[0], Ur[1], Ur[2], ihr, lF, &lUr[0], &lUr[1], &lUr[2]);
-      const double lhs = fma(lUs[1], uxs, fma(lUs[2], vys, lUs[0]));
-      const double luxs = lUs[1] * hs, lvys = lUs[2] * hs;
-      const double lX = lhs * iY, lY = -lX * hs;
-      lhr = fma(lX, A, lhr);
-      lA = fma(lX, hr, lA);
-      lar += lY;
-      lus -= lY;
-      lvr = fma(luxs, tx, lvys * nx);
-      lus = fma(luxs, ty, fma(lvys, ny, lus));
-      lhr = fma(lUr[1], R.u, fma(lUr[2], R.v, lhr + lUr[0]));
-      lRu = fma(lUr[1], hr, lRu);
-      lRv = fma(lUr[2], hr, lRv);
+    for (int q = 0; q < 3; ++q) {
+      lsx = fma(lF[q], Us[q] - Ux[q], lsx);
+      lUs[q] = sx * lF[q];
+      lUx[q] = -lUs[q];
+    }
+    double lax = (right ? dlt(0., ar) : dlt(al, 0.)) ? lsx : 0.;
+    elem_flux_rev(nx, ny, Ux[0], Ux[1], Ux[2], ihx, lF, &lUx[0], &lUx[1], &lUx[2]);
+    const double lhs = fma(lUs[1], uxs, fma(lUs[2], vys, lUs[0]));
+    const double luxs = lUs[1] * hs, lvys = lUs[2] * hs;
+    const double lX = lhs * iY, lY = -lX * hs;
+    double lhx = lX * Kx;
+    const double lKx = lX * hx;
+    lax += lY;
+    lus -= lY;
+    const double lvtx = fma(luxs, tx, lvys * nx);
+    lus = fma(luxs, ty, fma(lvys, ny, lus));
+    lhx = fma(lUx[1], X.u, fma(lUx[2], X.v, lhx + lUx[0]));
+    const double lux = lUx[1] * hx, lvx = lUx[2] * hx;
+    if (right) {
+      lhr += lhx;
+      lA += lKx;
+      lar += lax;
+      lvr = lvtx;
+      lRu += lux;
+      lRv += lvx;
     } else {
-      const double vl = fma(L.u, tx, L.v * ty);
-      const double ihl = is_wet(hl) ? SWE_DIV(1., hl) : 0.;
-      const double Ul[3] = {hl, hl * L.u, hl * L.v};
-      const double uxs = fma(vl, tx, us * ty);
-      const double vys = fma(vl, nx, us * ny);
-      const double iY = SWE_DIV(1., al - us);
-      const double hs = hl * B * iY;
-      const double Us[3] = {hs, hs * uxs, hs * vys};
-      const double sm = smin(0., al);
-      double lsm = 0., lUl[3], lUs[3];
-#pragma unroll
-      for (int q = 0; q < 3; ++q) {
-        lsm = fma(lF[q], Us[q] - Ul[q], lsm);
-        lUs[q] = sm * lF[q];
-        lUl[q] = -lUs[q];
-      }
-      if (dlt(al, 0.)) lal += lsm;
-      elem_flux_rev(nx, ny, Ul[0], Ul[1], Ul[2], ihl, lF, &lUl[0], &lUl[1], &lUl[2]);
-      const double lhs = fma(lUs[1], uxs, fma(lUs[2], vys, lUs[0]));
-      const double luxs = lUs[1] * hs, lvys = lUs[2] * hs;
-      const double lX = lhs * iY, lY = -lX * hs;
-      lhl = fma(lX, B, lhl);
-      lB = fma(lX, hl, lB);
-      lal += lY;
-      lus -= lY;
-      lvl = fma(luxs, tx, lvys * nx);
-      lus = fma(luxs, ty, fma(lvys, ny, lus));
-      lhl = fma(lUl[1], L.u, fma(lUl[2], L.v, lhl + lUl[0]));
-      lLu = fma(lUl[1], hl, lLu);
-      lLv = fma(lUl[2], hl, lLv);
+      lhl += lhx;
+      lB += lKx;
+      lal += lax;
+      lvl = lvtx;
+      lLu += lux;
+      lLv += lvx;
     }
     // us = N / D
     const double lN = lus * SWE_DIV(1., D);
