@@ -248,6 +248,14 @@ swe_status swe_batch_launch_count(swe_batch* b, int64_t* n);
 swe_status swe_batch_synchronize(swe_batch* b);
 const char* swe_batch_last_error(swe_batch* b);
 
+/* Volume, kinetic and potential energy of the current state:
+ * out3 = sum over wet cells of A (h, h (u^2 + v^2) / 2, h^2 / 2 + h b) with b
+ * the centroid bathymetry (the reference's ComputeIntegrals,
+ * src/SpaceDisc.cpp:76-104, commented out there; partially-wet cells use their
+ * cell average).  Deterministic.  Synchronises the context's stream. */
+swe_status swe_integrals(swe_ctx* ctx, double* out3);
+swe_status swe_batch_integrals(swe_batch* b, int32_t instance, double* out3);
+
 /* The discrete adjoint of a batch: as swe_adjoint_forward / _backward / _dts,
  * over all instances at once.  Cells, nodes and gauges are numbered over the
  * concatenation of the instances in creation order (instance q's cell i is

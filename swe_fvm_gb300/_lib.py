@@ -33,6 +33,7 @@ EXPORTS = [
     "swe_last_error", "swe_adjoint_forward", "swe_adjoint_backward", "swe_adjoint_dts", "swe_edge_fluxes_noalloc", "swe_batch_create", "swe_batch_destroy", "swe_batch_set_stream", "swe_batch_run_cfl", "swe_batch_run",
     "swe_batch_get_prim", "swe_batch_time", "swe_batch_launch_count", "swe_batch_synchronize",
     "swe_batch_last_error", "swe_batch_adjoint_forward", "swe_batch_adjoint_backward", "swe_batch_adjoint_dts",
+    "swe_integrals", "swe_batch_integrals",
 ]
 
 
@@ -129,6 +130,8 @@ def load(build_if_needed: bool = True):
         "swe_batch_adjoint_forward": [vp, i32, i64, i64, i32, vp, i64, vp],
         "swe_batch_adjoint_backward": [vp, vp, vp, vp],
         "swe_batch_adjoint_dts": [vp, vp],
+        "swe_integrals": [vp, vp],
+        "swe_batch_integrals": [vp, i32, vp],
     }
     for name, args in sig.items():
         f = getattr(L, name)

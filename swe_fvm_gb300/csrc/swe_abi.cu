@@ -313,6 +313,15 @@ swe_status swe_compute_fluxes(swe_ctx* ctx) {
   return SWE_OK;
 }
 
+swe_status swe_integrals(swe_ctx* ctx, double* out3) {
+  if (!ctx || !out3) return SWE_ERR_INVALID_ARGUMENT;
+  SWE_GUARD_BEGIN
+  cudaError_t e = ctx->eng.integrals(0, ctx->eng.C(), out3);
+  if (e != cudaSuccess) return cuda_fail(&ctx->err, e, "swe_integrals");
+  return SWE_OK;
+  SWE_GUARD_END(&ctx->err)
+}
+
 swe_status swe_get_prim(swe_ctx* ctx, double* prim_out) {
   if (!ctx || !prim_out) return SWE_ERR_INVALID_ARGUMENT;
   SWE_GUARD_BEGIN
@@ -612,6 +621,16 @@ swe_status swe_batch_adjoint_dts(swe_batch* b, double* dts_out) {
   std::string e = b->eng.adjoint_dts(dts_out);
   if (!e.empty()) return fail(&b->err, SWE_ERR_INVALID_ARGUMENT, e);
   return SWE_OK;
+}
+
+swe_status swe_batch_integrals(swe_batch* b, int32_t q, double* out3) {
+  if (!b || !out3 || q < 0 || q >= b->eng.I()) return SWE_ERR_INVALID_ARGUMENT;
+  SWE_GUARD_BEGIN
+  const int64_t c0 = b->eng.cell_off[q], n = b->eng.cell_off[q + 1] - c0;
+  cudaError_t e = b->eng.integrals(c0, n, out3);
+  if (e != cudaSuccess) return cuda_fail(&b->err, e, "swe_batch_integrals");
+  return SWE_OK;
+  SWE_GUARD_END(&b->err)
 }
 
 swe_status swe_batch_time(swe_batch* b, int32_t q, double* t) {

@@ -165,6 +165,8 @@ class Engine {
   cudaError_t adjoint_stage_reverse(const Stage& st, const double* const* in, const double* const* u0, AdjWork& aw);
   cudaError_t adjoint_stage_reverse_stored(const Stage& st, const double* const* in, const double* const* u0,
                                            AdjWork& aw, const DevWork& wk, const double* nst);
+  // volume, kinetic and potential energy of cells c0 .. c0+n-1 (host out[3])
+  cudaError_t integrals(int64_t c0, int64_t n, double* out_host);
   // the update kernel of one stage alone (the rest of the stage already ran),
   // also keeping the state before ConsAssigner in nst [3][C]
   cudaError_t update_only(const Stage& st, const double* const* in, const double* const* u0, double* const* out,
@@ -221,7 +223,8 @@ class Engine {
   cudaEvent_t ev_fork_ = nullptr, ev_join_ = nullptr;
   int flux_ = 1, ws_ = 2, block_ = 256;
   bool batched_ = false;
-  bool cor0_ = true;  // every instance has cor = 0: no Coriolis arithmetic in the reconstruction
+  bool cor0_ = true;
+  double* d_integrals_ = nullptr;  // partial sums of the integrals  // every instance has cor = 0: no Coriolis arithmetic in the reconstruction
   void launch_recon1(const double* W, const double* U, const double* V, int latch_mode);
   void launch_recon2(const double* W, const double* U, const double* V, cudaStream_t s);
   // fluxes: mode 0 every edge; mode 1 the edges with no partially-wet cell;

@@ -246,6 +246,13 @@ class SpaceDisc:
         self._check(_lib.load().swe_time_kernels(self.ctx, int(scheme), int(reps), out.ctypes.data))
         return out
 
+    def integrals(self) -> np.ndarray:
+        """(volume, kinetic energy, potential energy) of the current state,
+        summed on the device over the wet cells."""
+        out = np.zeros(3)
+        self._check(_lib.load().swe_integrals(self.ctx, out.ctypes.data))
+        return out
+
     def launch_count(self) -> int:
         n = ctypes.c_int64()
         self._check(_lib.load().swe_launch_count(self.ctx, ctypes.byref(n)))
@@ -361,6 +368,12 @@ class Batch:
         t = ctypes.c_double()
         self._check(_lib.load().swe_batch_time(self.b, int(q), ctypes.byref(t)))
         return t.value
+
+    def integrals(self, q: int) -> np.ndarray:
+        """(volume, kinetic, potential energy) of instance q."""
+        out = np.zeros(3)
+        self._check(_lib.load().swe_batch_integrals(self.b, int(q), out.ctypes.data))
+        return out
 
     def synchronize(self) -> None:
         self._check(_lib.load().swe_batch_synchronize(self.b))
