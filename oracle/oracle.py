@@ -23,13 +23,14 @@ SCHEME = {"Euler": 0, "SSPRK2": 1, "SSPRK3": 2}
 
 
 def build(force: bool = False) -> str:
-    """Compile the restatement with gcc: -O3, no FMA contraction, no -march."""
+    """Compile the restatement with gcc: -O3, no FMA contraction, no -march,
+    OpenMP for the optional jacobi-order threads."""
     os.makedirs(BUILD, exist_ok=True)
     if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(SRC):
         return LIB
     tmp = LIB + f".tmp{os.getpid()}"
-    subprocess.check_call(["gcc", "-O3", "-std=c11", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared",
-                           SRC, "-o", tmp, "-lm"])
+    subprocess.check_call(["gcc", "-O3", "-std=c11", "-ffp-contract=off", "-fno-fast-math", "-fopenmp", "-fPIC",
+                           "-shared", SRC, "-o", tmp, "-lm"])
     os.replace(tmp, LIB)
     return LIB
 
@@ -51,6 +52,7 @@ def lib():
         L.oracle_compute_fluxes.argtypes = [vp]
         L.oracle_min_len_to_wavespeed.argtypes = [vp]
         L.oracle_min_len_to_wavespeed.restype = d
+        L.oracle_set_threads.argtypes = [vp, i32]
         L.oracle_get_prim.argtypes = [vp, vp]
         L.oracle_set_prim.argtypes = [vp, vp]
         L.oracle_get_edge_fields.argtypes = [vp, vp, vp, vp, vp]
@@ -100,6 +102,10 @@ class Oracle:
 
     def min_len_to_wavespeed(self) -> float:
         return lib().oracle_min_len_to_wavespeed(self.ptr)
+
+    def set_threads(self, n: int) -> None:
+        """Run the jacobi-order loops on n OpenMP threads (results unchanged)."""
+        lib().oracle_set_threads(self.ptr, int(n))
 
     def prim(self) -> np.ndarray:
         out = np.empty((self.mesh.num_cells, 3))

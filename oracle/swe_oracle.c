@@ -28,6 +28,12 @@
  *   - std::cbrt (src/MUSCLObject.cpp:103) is replaced by the correctly rounded
  *     cube root (libm cube roots are faithful only and disagree in the last
  *     bit across libraries).
+ *
+ * Threads (jacobi order only, oracle_set_threads): the per-cell and per-edge
+ * loops run under OpenMP.  In jacobi order every write goes to the cell's or
+ * edge's own slots, the node maxima are an exact atomic max and the CFL ratio
+ * a min reduction, so the results equal one thread's bit for bit.  Literal
+ * order always runs on one thread (its results depend on the cell order).
  *   - (int)log2(b - a) in Bisection is taken exactly from the binary exponent.
  *
  * Build: -O2 -ffp-contract=off (no FMA contraction, so results do not depend on
@@ -78,6 +84,7 @@ typedef struct oracle_ctx {
   double* geom;
   int64_t *en, *ec, *cn, *ce, *ct;
   int flux, ws, order;
+  int threads; /* jacobi-order loops run on this many OpenMP threads */
   double cor, tau;
   double* vol;      /* 3 x C prim (w,u,v) */
   double* vol_snap; /* start-of-stage snapshot (jacobi reads) */
@@ -547,6 +554,25 @@ static muscl_t ReconstructPartWetCell2(const oracle_ctx* c, int64_t i) {
 
 /* ------------------------------------------------------------- SpaceDisc */
 /* src/SpaceDisc.cpp:15-31 */
+/* max_wp[n] = smax(max_wp[n], v), exactly, when other threads update it too */
+static void node_max(oracle_ctx* c, int64_t n, double v) {
+  if (c->threads <= 1 || c->order != ORACLE_ORDER_JACOBI) {
+    c->max_wp[n] = smax(c->max_wp[n], v);
+    return;
+  }
+  uint64_t* p = (uint64_t*)(c->max_wp + n);
+  uint64_t ob = __atomic_load_n(p, __ATOMIC_RELAXED), nb;
+  memcpy(&nb, &v, sizeof nb);
+  for (;;) {
+    double od;
+    memcpy(&od, &ob, sizeof od);
+    if (!(od < v)) return;
+    if (__atomic_compare_exchange_n(p, &ob, nb, 0, __ATOMIC_RELAXED, __ATOMIC_RELAXED)) return;
+  }
+}
+
+static int parallel(const oracle_ctx* c) { return c->threads > 1 && c->order == ORACLE_ORDER_JACOBI; }
+
 static void UpdateInterfaceValues(oracle_ctx* c, const muscl_t* m) {
   int64_t i = m->i;
   const int64_t* ip = c->cn + 3 * i;
@@ -555,7 +581,7 @@ static void UpdateInterfaceValues(oracle_ctx* c, const muscl_t* m) {
   for (int k = 0; k < 3; ++k) {
     double ap[3];
     muscl_at_point(c, m, P(c, ip[k]), ap);
-    c->max_wp[ip[k]] = smax(c->max_wp[ip[k]], ap[0]);
+    node_max(c, ip[k], ap[0]);
     double ec[3];
     E(c, ie[k], ec);
     double ae[3];
@@ -577,6 +603,7 @@ void oracle_compute_interface_values(oracle_ctx* c) {
   const int64_t N = c->m.num_nodes, C = c->m.num_cells;
   for (int64_t n = 0; n < N; ++n) c->max_wp[n] = c->geom[3 * n + 2];
   c->vol_read = c->vol;
+#pragma omp parallel for schedule(dynamic, 4096) if (parallel(c)) num_threads(c->threads)
   for (int64_t i = 0; i < C; ++i) {
     muscl_t m;
     if (IsDryCell(c, i)) m = ReconstructDryCell(c, i);
@@ -590,6 +617,7 @@ void oracle_compute_interface_values(oracle_ctx* c) {
   } else {
     c->maxwp_read = c->max_wp;
   }
+#pragma omp parallel for schedule(dynamic, 4096) if (parallel(c)) num_threads(c->threads)
   for (int64_t i = 0; i < C; ++i) {
     if (IsPartWetCell(c, i)) {
       muscl_t m = ReconstructPartWetCell2(c, i);
@@ -719,8 +747,9 @@ static void FluxHLLC(oracle_ctx* c, int64_t e, int64_t from, int64_t to, double*
 
 /* src/SpaceDisc.cpp:54-74 */
 void oracle_compute_fluxes(oracle_ctx* c) {
-  c->r = 1.;
+  double r = 1.;
   const int64_t E_ = c->m.num_edges;
+#pragma omp parallel for schedule(dynamic, 4096) reduction(min : r) if (parallel(c)) num_threads(c->threads)
   for (int64_t e = 0; e < E_; ++e) {
     int64_t lf = c->ec[2 * e], lt = c->ec[2 * e + 1];
     double n[2];
@@ -730,11 +759,12 @@ void oracle_compute_fluxes(oracle_ctx* c) {
       double U[3] = {vol_h(c, c->vol, lf), 0., 0.};
       ElemFlux(n, U, fo);
     } else if (c->flux == FLUX_HLL) {
-      FluxHLL(c, e, lf, lt, &c->r, fo);
+      FluxHLL(c, e, lf, lt, &r, fo);
     } else {
-      FluxHLLC(c, e, lf, lt, &c->r, fo);
+      FluxHLLC(c, e, lf, lt, &r, fo);
     }
   }
+  c->r = r;
 }
 
 /* ------------------------------------------------------------- TimeDisc */
@@ -798,6 +828,7 @@ static void rk_stage(oracle_ctx* c, const double* u0, int first, double a, doubl
   } else {
     c->vol_read = c->vol;
   }
+#pragma omp parallel for schedule(dynamic, 4096) if (parallel(c)) num_threads(c->threads)
   for (int64_t i = 0; i < C; ++i) {
     double rhs[3], U0[3], nv[3];
     RHS(c, i, dt_stage, rhs);
@@ -837,6 +868,8 @@ void oracle_step(oracle_ctx* c, int scheme, double dt) {
 /* include/TimeDisc.h:13,22 with the coefficient as a parameter */
 double oracle_min_len_to_wavespeed(const oracle_ctx* c) { return c->r; }
 
+void oracle_set_threads(oracle_ctx* c, int n) { c->threads = n > 1 ? n : 1; }
+
 static int64_t* dup_i64(const int64_t* p, int64_t n) {
   int64_t* q = (int64_t*)malloc((size_t)(n > 0 ? n : 1) * sizeof(int64_t));
   if (n > 0) memcpy(q, p, (size_t)n * sizeof(int64_t));
@@ -863,6 +896,7 @@ oracle_ctx* oracle_create(int64_t num_nodes, int64_t num_edges, int64_t num_cell
   c->cor = cor;
   c->tau = tau;
   c->order = order;
+  c->threads = 1;
   c->vol = (double*)malloc((size_t)num_cells * 3 * sizeof(double));
   c->vol_snap = (double*)malloc((size_t)num_cells * 3 * sizeof(double));
   /* SpaceDisc copies v0 through the volume field (src/MUSCLObject.cpp:8-11) */

@@ -183,3 +183,22 @@ def test_cbrt_correctly_rounded():
         # y is nearest: (y+lo)/2 <= cbrt(x) <= (y+hi)/2, compared by cubing
         assert ((fy + lo) / 2) ** 3 <= fx <= ((fy + hi) / 2) ** 3, x
     assert L.oracle_cbrt_rn(-8.0) == -2.0 and L.oracle_cbrt_rn(0.0) == 0.0
+
+
+def test_threaded_jacobi_oracle_equals_one_thread():
+    """The OpenMP jacobi loops (exact atomic node maxima, min-reduced CFL ratio)
+    give the single-thread results bit for bit."""
+    from swe_fvm_gb300 import scenarios
+
+    m, prim = scenarios.random_front_case(24, 3)
+    a, b = Oracle(m, prim), Oracle(m, prim)
+    b.set_threads(4)
+    for o in (a, b):
+        o.compute_interface_values()
+        o.compute_fluxes()
+    for _ in range(6):
+        dt = 0.15 * a.min_len_to_wavespeed()
+        assert dt == 0.15 * b.min_len_to_wavespeed()
+        a.step("SSPRK2", dt)
+        b.step("SSPRK2", dt)
+    assert np.array_equal(a.prim(), b.prim())
