@@ -241,6 +241,20 @@ def run_gpu(args):
            "d2h_bytes_per_step": 24 * C, "steps": n_e2e,
            "api": "swe_set_prim + swe_step + swe_get_prim (pinned host buffers)"}
 
+    # the same workload with the HLL plugin (the configuration names HLL and HLLC)
+    sd_hll = SpaceDisc(Fluxes.HLL(Wavespeeds.Einfeldt), mesh, prim, cfl=CFL)
+    sd_hll.set_stream(stream.cuda_stream)
+    sd_hll.run_cfl(1, args.warmup)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    _lib.check(_lib.load().swe_run_cfl(sd_hll.ctx, 1, args.steps, None), sd_hll.ctx)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms_hll = e0.elapsed_time(e1)
+    hll = {"value": world * C * args.steps / (ms_hll * 1e-3), "unit": "cell-updates/s",
+           "ms_per_step": ms_hll / args.steps, "flux": "HLL+Einfeldt"}
+    del sd_hll
+
     fp64 = ctypes.c_double(0.0)
     _lib.check(L.swe_measure_fp64_peak(ctypes.byref(fp64)))
     hbm, src = peaks()
@@ -261,7 +275,7 @@ def run_gpu(args):
                    "flux": "HLLC+Einfeldt", "scheme": "SSPRK2", "cfl": CFL, "dt": "CFLdt() per step, on device",
                    "l2": "working set > 1 GB, larger than the 129 MB L2; no flush",
                    "parallelism": f"replicas x{world}", "mesh_gen_s": round(t_gen, 1)},
-        "e2e": e2e, "gpu_launches": launches, "roofline": roof, "clocks": clk.summary(),
+        "e2e": e2e, "gpu_launches": launches, "roofline": roof, "clocks": clk.summary(), "hll": hll,
     }
     if ENSEMBLE_INSTANCES > 0 and not args.no_ensemble:
         out["batched"] = run_ensemble(torch, stream)

@@ -2,8 +2,8 @@
 
 Tolerances (FP64): per-step relative L2 of the primitive field <= 1e-12 and
 final-time relative L2 <= 1e-10.  With the default build (no FMA fusion on the
-device, reference operation order) the two agree bit for bit except where
-cbrt's last bit differs between the CUDA and host math libraries.
+device, the reference's operation order, correctly rounded division, square
+and cube roots on both sides) the two agree bit for bit.
 """
 import numpy as np
 import pytest
