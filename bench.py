@@ -128,16 +128,39 @@ def cpu_baseline(mesh, prim, budget_s: float = 10.0):
 
 
 def dist_setup(n_gpus):
+    """Replicas only: one process per GPU, no collective on the data path.
+    NCCL on GPUs; gloo when no GPU is visible (the CPU tests of this logic)."""
     import torch
 
     if n_gpus > 1 or "WORLD_SIZE" in os.environ:
         import torch.distributed as dist
 
         local = int(os.environ.get("LOCAL_RANK", "0"))
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
+            dist.init_process_group("nccl")
+        else:
+            dist.init_process_group("gloo")
         return dist, dist.get_rank(), dist.get_world_size(), local
     return None, 0, 1, 0
+
+
+def max_over_ranks(ms, dist):
+    """The slowest rank's time (the whole job's time for weak-scaled replicas)."""
+    if not dist:
+        return ms
+    import torch
+
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([ms], device=dev, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.barrier()
+    return float(t.item())
+
+
+def job_rate(world, cells, steps, ms):
+    """Whole-job cell-updates/s: every rank advanced its own replica."""
+    return world * cells * steps / (ms * 1e-3)
 
 
 def run_gpu(args):
@@ -206,13 +229,9 @@ def run_gpu(args):
         torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)
     launches = sd.launch_count() - n0
-    if dist:
-        t = torch.tensor([ms], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-        dist.barrier()
+    ms = max_over_ranks(ms, dist)
     sd.synchronize()
-    value = world * C * args.steps / (ms * 1e-3)
+    value = job_rate(world, C, args.steps, ms)
     ms_step = ms / args.steps
 
     # per-kernel CUDA-event timings (kernel by kernel, same stream)
