@@ -293,7 +293,8 @@ def run_gpu(args):
         "config": {"workload": "dam_break_1M", "cells": C, "edges": mesh.num_edges, "nodes": mesh.num_nodes,
                    "flux": "HLLC+Einfeldt", "scheme": "SSPRK2", "cfl": CFL, "dt": "CFLdt() per step, on device",
                    "l2": "working set > 1 GB, larger than the 129 MB L2; no flush",
-                   "parallelism": f"replicas x{world}", "mesh_gen_s": round(t_gen, 1)},
+                   "parallelism": f"replicas x{world}", "mesh_gen_s": round(t_gen, 1),
+                   "tuning": sd.tuning()},
         "e2e": e2e, "gpu_launches": launches, "roofline": roof, "clocks": clk.summary(), "hll": hll,
     }
     if ENSEMBLE_INSTANCES > 0 and not args.no_ensemble:
@@ -302,12 +303,45 @@ def run_gpu(args):
         out["adjoint"] = run_adjoint(torch, stream)
     if BADJ_INSTANCES > 0 and not args.no_batch_adjoint:
         out["batched_adjoint"] = run_batch_adjoint(torch, stream)
+    if args.layouts:
+        out["layouts"] = run_layouts(torch, stream, mesh, prim, args.steps, args.warmup)
     if rank == 0:
         if world == 1 and not args.no_cpu:
             out["cpu_baseline"] = cpu_baseline(mesh, prim)
         print(json.dumps(out), flush=True)
     if dist:
         dist.destroy_process_group()
+
+
+def run_layouts(torch, stream, mesh, prim, steps, warmup):
+    """Plain SSPRK2 step time of the same mesh in each device order, and of a
+    copy numbered at random (caller's order kept vs the tuner's choice)."""
+    from swe_fvm_gb300 import Fluxes, SpaceDisc, Wavespeeds, _lib
+    from swe_fvm_gb300.mesh import shuffled
+
+    smesh, cf, _, _ = shuffled(mesh, 123)
+    sprim = prim[cf]
+    cases = [("generated/keep", mesh, prim, "keep"), ("generated/morton", mesh, prim, "morton"),
+             ("generated/rcm", mesh, prim, "rcm"), ("generated/auto", mesh, prim, "auto"),
+             ("shuffled/keep", smesh, sprim, "keep"), ("shuffled/auto", smesh, sprim, "auto")]
+    out = {}
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for label, m, p, reorder in cases:
+        t0 = time.perf_counter()
+        sd = SpaceDisc(Fluxes.HLLC(Wavespeeds.Einfeldt), m, p, cfl=CFL, reorder=reorder)
+        t_create = time.perf_counter() - t0
+        sd.set_stream(stream.cuda_stream)
+        sd.run_cfl(1, warmup)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        _lib.check(_lib.load().swe_run_cfl(sd.ctx, 1, steps, None), sd.ctx)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        out[label] = {"ms_per_step": ms, "cell_updates_per_s": m.num_cells / (ms * 1e-3), "tuning": sd.tuning(),
+                      "create_s": round(t_create, 2)}
+        del sd
+    return out
 
 
 ENSEMBLE_INSTANCES = int(os.environ.get("SWE_BENCH_ENSEMBLE", "256"))
@@ -557,6 +591,7 @@ def main():
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint leg")
     ap.add_argument("--adjoint-profile", action="store_true", help="only a short taped run and its reverse")
     ap.add_argument("--no-batch-adjoint", action="store_true", help="skip the batched-adjoint leg")
+    ap.add_argument("--layouts", action="store_true", help="also time every device order of the mesh")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

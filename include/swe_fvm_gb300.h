@@ -49,6 +49,25 @@ typedef enum swe_status {
 typedef enum swe_flux { SWE_FLUX_HLL = 0, SWE_FLUX_HLLC = 1 } swe_flux;
 /* Wave-speed plugin: Wavespeeds::Rusanov / Davis / Einfeldt (src/Fluxes.cpp:5-26). */
 typedef enum swe_wavespeed { SWE_WS_RUSANOV = 0, SWE_WS_DAVIS = 1, SWE_WS_EINFELDT = 2 } swe_wavespeed;
+/* Device order of an instance's cells, edges and nodes.  The reference has
+ * one order, the caller's (include/TriangMesh.h:14-65); every array crossing
+ * this boundary stays in the caller's order whatever the device uses, and
+ * states are bit-identical in every order (each cell and edge is computed
+ * from its own topology row).  MORTON sorts cells by the z-order of their
+ * centroids, RCM by reverse Cuthill-McKee over the cell-neighbour graph;
+ * edges follow their owner cell, nodes their first cell.  AUTO (the default)
+ * picks one of KEEP, MORTON, RCM: for meshes of 65,536 cells or more
+ * swe_create builds a context in each order and keeps the one whose SSPRK2
+ * steps run fastest (the caller's order unless another is more than 2 %
+ * faster); smaller meshes and batch instances take the one with the fewest
+ * 32-byte sectors gathered per warp (the caller's order unless another saves
+ * more than 5 %). */
+typedef enum swe_reorder {
+  SWE_REORDER_AUTO = -1,
+  SWE_REORDER_KEEP = 0,
+  SWE_REORDER_MORTON = 1,
+  SWE_REORDER_RCM = 2
+} swe_reorder;
 /* Time scheme: Solvers::Euler / SSPRK2 / SSPRK3 (src/Solvers.cpp:5-59). */
 typedef enum swe_scheme { SWE_SCHEME_EULER = 0, SWE_SCHEME_SSPRK2 = 1, SWE_SCHEME_SSPRK3 = 2 } swe_scheme;
 
@@ -74,8 +93,9 @@ typedef struct swe_params {
   double cor;        /* Coriolis parameter (SpaceDisc::m_cor) */
   double tau;        /* friction (stored, unused by the reference: src/TimeDisc.cpp:38-39) */
   double cfl;        /* TimeDisc::CFLdt() = cfl * min length-to-wavespeed ratio */
-  int32_t reorder;   /* 0: keep the caller's cell order, 1: Morton order internally */
-  int32_t block;     /* threads per block for the cell/edge kernels; 0 = tuned default */
+  int32_t reorder;   /* swe_reorder: device order of cells, edges and nodes (default AUTO) */
+  int32_t block;     /* threads per block of the cell and edge kernels: 0 = timed at creation
+                        (default), else a multiple of 32 from 32 to 256 */
 } swe_params;
 
 typedef struct swe_ctx swe_ctx;
@@ -178,6 +198,22 @@ swe_status swe_synchronize(swe_ctx* ctx);
  * on this thread).  Never NULL. */
 const char* swe_last_error(swe_ctx* ctx);
 
+/* What the tuner chose: out4 = {device order (swe_reorder), threads per block
+ * of the reconstruction kernels, of the edge-flux kernel, of the drain and
+ * update kernels}.  Block sizes are timed at creation when swe_params.block
+ * is 0 (64, 128 and 256 threads; steps run on a copy of the state, which is
+ * then restored) and cached per device, flux, wave speed and log2 of the
+ * cell count.  No reference counterpart (the reference has no tuner). */
+swe_status swe_get_tuning(swe_ctx* ctx, int32_t* out4);
+
+/* Host-only planning of a device order (AUTO: the cost-model choice):
+ * cell_from[C], edge_from[E], node_from[N] (each optional) receive the
+ * caller's index at every device position; cost3 (optional) the gathered
+ * sectors of KEEP, MORTON and RCM (AUTO fills all three, a fixed strategy its
+ * own); chosen the strategy used.  Needs no GPU. */
+swe_status swe_layout_plan(const swe_mesh* mesh, int32_t strategy, int64_t* cell_from, int64_t* edge_from,
+                           int64_t* node_from, double* cost3, int32_t* chosen);
+
 /* Edge-flux pass that allocates no device memory, for callers that cannot call
  * cudaMalloc (a framework owning all device memory through its own pool, a
  * real-time loop that forbids allocation, a plugin handed only device
@@ -245,6 +281,8 @@ swe_status swe_batch_get_prim(swe_batch* b, int32_t instance, double* prim_out);
 /* Sum of the dts taken by an instance so far. */
 swe_status swe_batch_time(swe_batch* b, int32_t instance, double* t);
 swe_status swe_batch_launch_count(swe_batch* b, int64_t* n);
+/* swe_get_tuning for instance q of a batch (block sizes are shared). */
+swe_status swe_batch_get_tuning(swe_batch* b, int32_t q, int32_t* out4);
 swe_status swe_batch_synchronize(swe_batch* b);
 const char* swe_batch_last_error(swe_batch* b);
 

@@ -33,7 +33,7 @@ EXPORTS = [
     "swe_last_error", "swe_adjoint_forward", "swe_adjoint_backward", "swe_adjoint_dts", "swe_edge_fluxes_noalloc", "swe_batch_create", "swe_batch_destroy", "swe_batch_set_stream", "swe_batch_run_cfl", "swe_batch_run",
     "swe_batch_get_prim", "swe_batch_time", "swe_batch_launch_count", "swe_batch_synchronize",
     "swe_batch_last_error", "swe_batch_adjoint_forward", "swe_batch_adjoint_backward", "swe_batch_adjoint_dts",
-    "swe_integrals", "swe_batch_integrals",
+    "swe_integrals", "swe_batch_integrals", "swe_get_tuning", "swe_batch_get_tuning", "swe_layout_plan",
 ]
 
 
@@ -132,6 +132,9 @@ def load(build_if_needed: bool = True):
         "swe_batch_adjoint_dts": [vp, vp],
         "swe_integrals": [vp, vp],
         "swe_batch_integrals": [vp, i32, vp],
+        "swe_get_tuning": [vp, vp],
+        "swe_batch_get_tuning": [vp, i32, vp],
+        "swe_layout_plan": [vp, i32, vp, vp, vp, vp, P(i32)],
     }
     for name, args in sig.items():
         f = getattr(L, name)

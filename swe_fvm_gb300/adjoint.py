@@ -22,9 +22,10 @@ from .solver import Batch, Fluxes, SpaceDisc, Wavespeeds
 class Rollout:
     """A taped forward run and its adjoint, without PyTorch."""
 
-    def __init__(self, mesh: Mesh, prim0, fluxer=None, cfl=0.15, cor=0.0):
+    def __init__(self, mesh: Mesh, prim0, fluxer=None, cfl=0.15, cor=0.0, reorder="auto", block=0):
         self.mesh = mesh.contiguous()
-        self.sd = SpaceDisc(fluxer or Fluxes.HLLC(Wavespeeds.Einfeldt), self.mesh, prim0, cor=cor, cfl=cfl)
+        self.sd = SpaceDisc(fluxer or Fluxes.HLLC(Wavespeeds.Einfeldt), self.mesh, prim0, cor=cor, cfl=cfl,
+                            reorder=reorder, block=block)
 
     def forward(self, scheme: int, n_steps: int, checkpoint_every: int, gauges, obs_every: int) -> np.ndarray:
         g = np.ascontiguousarray(gauges, dtype=np.int64)
@@ -54,9 +55,9 @@ class BatchRollout:
     instances: one launch per stage kernel over all of them, each instance with
     its own CFL dt, gauges and gradients."""
 
-    def __init__(self, meshes, prims, fluxer=None, cfl=0.15, cor=0.0):
+    def __init__(self, meshes, prims, fluxer=None, cfl=0.15, cor=0.0, reorder="auto", block=0):
         self.meshes = [m.contiguous() for m in meshes]
-        self.batch = Batch(self.meshes, prims, fluxer=fluxer, cor=cor, cfl=cfl)
+        self.batch = Batch(self.meshes, prims, fluxer=fluxer, cor=cor, cfl=cfl, reorder=reorder, block=block)
         self.cell_off = np.concatenate([[0], np.cumsum([m.num_cells for m in self.meshes])]).astype(np.int64)
         self.node_off = np.concatenate([[0], np.cumsum([m.num_nodes for m in self.meshes])]).astype(np.int64)
         self.gauge_counts = []

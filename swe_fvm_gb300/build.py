@@ -20,7 +20,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libswe_gb300.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 SOURCES = ["swe_kernels.cu", "swe_precompute.cu", "swe_abi.cu", "swe_fp64_peak.cu", "swe_noalloc.cu", "swe_adjoint.cu",
-           "swe_diagnostics.cu"]
+           "swe_diagnostics.cu", "swe_layout.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -6,6 +6,7 @@
 // DomainError / SolverError / std::runtime_error, include/Exceptions.h:4-10).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <exception>
@@ -15,6 +16,7 @@
 
 #include "../../include/swe_fvm_gb300.h"
 #include "swe_engine.cuh"
+#include "swe_layout.cuh"
 
 using swe::Engine;
 using swe::HostInstance;
@@ -48,21 +50,25 @@ swe_status cuda_fail(std::string* slot, cudaError_t e, const char* where) {
 }
 
 // Interleave / de-interleave between the reference's 3 x C column-major
-// primitive field and the engine's three component arrays.
+// primitive field (the caller's cell order) and the engine's three component
+// arrays (device order; from[i] = the caller's row of device cell i, or null
+// when the two orders agree).
 __global__ void k_pack(const double* __restrict__ W, const double* __restrict__ U, const double* __restrict__ V,
-                       double* __restrict__ out, int n) {
+                       double* __restrict__ out, int n, const int* __restrict__ from) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) {
-    out[3 * i] = W[i];
-    out[3 * i + 1] = U[i];
-    out[3 * i + 2] = V[i];
+    const int r = from ? from[i] : i;
+    out[3 * r] = W[i];
+    out[3 * r + 1] = U[i];
+    out[3 * r + 2] = V[i];
   }
 }
 __global__ void k_unpack(const double* __restrict__ in, double* __restrict__ W, double* __restrict__ U,
-                         double* __restrict__ V, int n, unsigned* bad) {
+                         double* __restrict__ V, int n, unsigned* bad, const int* __restrict__ from) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) {
-    const double w = in[3 * i], u = in[3 * i + 1], v = in[3 * i + 2];
+    const int r = from ? from[i] : i;
+    const double w = in[3 * r], u = in[3 * r + 1], v = in[3 * r + 2];
     W[i] = w;
     U[i] = u;
     V[i] = v;
@@ -98,6 +104,74 @@ swe_status read_instance(const swe_mesh* m, const swe_params* p, HostInstance* h
   return SWE_OK;
 }
 
+// Validates one instance in the caller's numbering (so that messages name the
+// caller's indices), then picks its device layout and rewrites it in that
+// order.
+swe_status lay_out(HostInstance* h, int strategy, swe::Layout* L, std::string* why) {
+  std::string err = swe::validate_instance(*h);
+  if (!err.empty()) {
+    *why = err;
+    return SWE_ERR_INVALID_MESH;
+  }
+  if (strategy == swe::kLayoutKeep) {
+    *L = swe::Layout{};
+    return SWE_OK;
+  }
+  HostInstance o;
+  *L = swe::choose_layout(*h, strategy, nullptr, &o);
+  if (!L->identity()) *h = std::move(o);
+  return SWE_OK;
+}
+
+// Device position of the caller's (global) cell index.
+int64_t device_cell(const Engine& g, int64_t c) {
+  const size_t q = std::upper_bound(g.cell_off.begin(), g.cell_off.end(), c) - g.cell_off.begin() - 1;
+  const int64_t c0 = g.cell_off[q];
+  const swe::Layout& L = g.layouts[q];
+  return L.identity() ? c : c0 + L.cell_to[c - c0];
+}
+
+// Device-ordered rows (w values per cell or node, instances concatenated) to
+// the caller's order.
+void cells_to_caller(const Engine& g, const double* dev, double* out, int w) {
+  for (size_t q = 0; q < g.layouts.size(); ++q) {
+    const int64_t c0 = g.cell_off[q], n = g.cell_off[q + 1] - c0;
+    const swe::Layout& L = g.layouts[q];
+    for (int64_t j = 0; j < n; ++j) {
+      const int64_t d = c0 + (L.identity() ? j : L.cell_from[j]);
+      for (int c = 0; c < w; ++c) out[w * d + c] = dev[w * (c0 + j) + c];
+    }
+  }
+}
+void nodes_to_caller(const Engine& g, const double* dev, double* out) {
+  for (size_t q = 0; q < g.layouts.size(); ++q) {
+    const int64_t n0 = g.node_off[q], n = g.node_off[q + 1] - n0;
+    const swe::Layout& L = g.layouts[q];
+    for (int64_t j = 0; j < n; ++j) out[n0 + (L.identity() ? j : L.node_from[j])] = dev[n0 + j];
+  }
+}
+bool reordered(const Engine& g) { return g.d_cell_from != nullptr; }
+
+// Engine::adjoint_backward with its per-cell and per-node gradients returned
+// in the caller's order.
+std::string adjoint_backward_caller(Engine& g, const double* trace_grads, double* grad_prim0, double* grad_z) {
+  if (!reordered(g)) return g.adjoint_backward(trace_grads, grad_prim0, grad_z);
+  std::vector<double> gp(3 * (size_t)g.C()), gz((size_t)g.N());
+  std::string e = g.adjoint_backward(trace_grads, gp.data(), gz.data());
+  if (!e.empty()) return e;
+  cells_to_caller(g, gp.data(), grad_prim0, 3);
+  nodes_to_caller(g, gz.data(), grad_z);
+  return "";
+}
+
+// Times the block sizes (swe_params.block == 0) and re-primes the flux pass.
+swe_status tune(Engine& eng, std::string* err);
+
+// Meshes from this many cells up choose their device order (SWE_REORDER_AUTO)
+// by timing each candidate; smaller ones by the gather cost model.
+constexpr int64_t kTimedLayoutCells = 1 << 16;
+constexpr int kTimedLayoutSteps = 10;
+
 swe_status check_params(const swe_params* p, std::string* why) {
   if (p->flux < 0 || p->flux > 1) {
     *why = "flux must be SWE_FLUX_HLL or SWE_FLUX_HLLC";
@@ -107,9 +181,13 @@ swe_status check_params(const swe_params* p, std::string* why) {
     *why = "wavespeed must be SWE_WS_RUSANOV, SWE_WS_DAVIS or SWE_WS_EINFELDT";
     return SWE_ERR_INVALID_ARGUMENT;
   }
-  if (p->reorder != 0) {
-    *why = "reorder: only 0 (the caller's cell order) is implemented";
-    return SWE_ERR_UNSUPPORTED;
+  if (p->reorder < SWE_REORDER_AUTO || p->reorder > SWE_REORDER_RCM) {
+    *why = "reorder must be SWE_REORDER_AUTO, SWE_REORDER_KEEP, SWE_REORDER_MORTON or SWE_REORDER_RCM";
+    return SWE_ERR_INVALID_ARGUMENT;
+  }
+  if (p->block != 0 && (p->block < 32 || p->block > 256 || p->block % 32 != 0)) {
+    *why = "block must be 0 (tuned) or a multiple of 32 from 32 to 256";
+    return SWE_ERR_INVALID_ARGUMENT;
   }
   return SWE_OK;
 }
@@ -123,7 +201,8 @@ swe_status upload_prim(Engine& eng, const double* prim, int64_t c0, int64_t n, s
     e = cudaMemcpyAsync(eng.d_io, prim, 3 * n * sizeof(double), cudaMemcpyHostToDevice, eng.stream());
   if (e == cudaSuccess) {
     k_unpack<<<(int)((n + 255) / 256), 256, 0, eng.stream()>>>(eng.d_io, eng.state(0, 0) + c0, eng.state(0, 1) + c0,
-                                                                eng.state(0, 2) + c0, (int)n, flag);
+                                                                eng.state(0, 2) + c0, (int)n, flag,
+                                                                eng.d_cell_from ? eng.d_cell_from + c0 : nullptr);
     e = cudaGetLastError();
   }
   unsigned h = 0;
@@ -136,7 +215,8 @@ swe_status upload_prim(Engine& eng, const double* prim, int64_t c0, int64_t n, s
 
 swe_status download_prim(Engine& eng, double* prim, int64_t c0, int64_t n, std::string* err) {
   k_pack<<<(int)((n + 255) / 256), 256, 0, eng.stream()>>>(eng.state(0, 0) + c0, eng.state(0, 1) + c0,
-                                                            eng.state(0, 2) + c0, eng.d_io, (int)n);
+                                                            eng.state(0, 2) + c0, eng.d_io, (int)n,
+                                                            eng.d_cell_from ? eng.d_cell_from + c0 : nullptr);
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(prim, eng.d_io, 3 * n * sizeof(double), cudaMemcpyDeviceToHost, eng.stream());
@@ -166,6 +246,78 @@ swe_status prime(Engine& eng, std::string* err) {
   return SWE_OK;
 }
 
+swe_status tune(Engine& eng, std::string* err) {
+  cudaError_t e = eng.autotune_blocks(1);
+  if (e != cudaSuccess) return cuda_fail(err, e, "tuning the block sizes");
+  return prime(eng, err);
+}
+
+// A context over one validated instance already in the device order of L.
+swe_status build_ctx(HostInstance&& h, swe::Layout&& L, const swe_params& p, const double* prim0,
+                     std::unique_ptr<swe_ctx>* out, std::string* why) {
+  std::unique_ptr<swe_ctx> ctx(new swe_ctx());
+  ctx->flux = p.flux;
+  ctx->ws = p.wavespeed;
+  ctx->cfl = p.cfl;
+  int ist = 0;
+  const int64_t C = h.C;
+  std::vector<HostInstance> inst(1);
+  inst[0] = std::move(h);
+  std::string e = ctx->eng.init(std::move(inst), p.flux, p.wavespeed, p.block, &ist, false);
+  if (!e.empty()) return fail(why, (swe_status)ist, e);
+  std::vector<swe::Layout> lay(1);
+  lay[0] = std::move(L);
+  e = ctx->eng.set_layouts(std::move(lay));
+  if (!e.empty()) return fail(why, SWE_ERR_CUDA, e);
+  swe_status st = upload_prim(ctx->eng, prim0, 0, C, why);
+  if (st == SWE_OK) st = prime(ctx->eng, why);
+  if (st == SWE_OK && p.block == 0) st = tune(ctx->eng, why);
+  if (st != SWE_OK) return st;
+  *out = std::move(ctx);
+  return SWE_OK;
+}
+
+// SWE_REORDER_AUTO on a large mesh: builds a context in each order (the
+// caller's, Morton, RCM), times kTimedLayoutSteps graph-replayed SSPRK2 steps
+// of each from the initial state (twice, keeping the faster), and keeps the
+// fastest; another order replaces the current best only when it is more than
+// 2 % faster.  At most two contexts exist at once, and a candidate is skipped
+// when the device has no room for it beside the best one.
+swe_status create_timed(const HostInstance& h, const swe_params& p, const double* prim0,
+                        std::unique_ptr<swe_ctx>* out, std::string* why) {
+  static const int kCand[3] = {SWE_REORDER_KEEP, SWE_REORDER_MORTON, SWE_REORDER_RCM};
+  std::unique_ptr<swe_ctx> best;
+  float best_ms = 0.f;
+  for (int s : kCand) {
+    if (best) {
+      size_t free_b = 0, total_b = 0;
+      if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) break;
+      if (free_b < best->eng.device_bytes() + best->eng.device_bytes() / 4 + (size_t(256) << 20)) break;
+    }
+    swe::Layout L = swe::make_layout(h, s);
+    HostInstance d = L.identity() ? h : swe::apply_layout(h, L);
+    std::unique_ptr<swe_ctx> c;
+    swe_status st = build_ctx(std::move(d), std::move(L), p, prim0, &c, why);
+    if (st != SWE_OK) {
+      if (best) break;  // keep what already works
+      return st;
+    }
+    float ms = 0.f, ms2 = 0.f;
+    cudaError_t e = c->eng.time_steps(1, kTimedLayoutSteps, &ms);
+    if (e == cudaSuccess) e = c->eng.time_steps(1, kTimedLayoutSteps, &ms2);
+    if (e != cudaSuccess) return cuda_fail(why, e, "timing a device order");
+    st = prime(c->eng, why);
+    if (st != SWE_OK) return st;
+    ms = std::min(ms, ms2);
+    if (!best || ms < 0.98f * best_ms) {
+      best = std::move(c);
+      best_ms = ms;
+    }
+  }
+  *out = std::move(best);
+  return SWE_OK;
+}
+
 #define SWE_GUARD_BEGIN try {
 #define SWE_GUARD_END(slot)                                           \
   }                                                                   \
@@ -187,7 +339,7 @@ swe_status swe_params_default(swe_params* p) {
   p->cor = 0.;
   p->tau = 0.;
   p->cfl = 0.15;
-  p->reorder = 0;
+  p->reorder = SWE_REORDER_AUTO;
   p->block = 0;
   return SWE_OK;
 }
@@ -203,20 +355,19 @@ swe_status swe_create(const swe_mesh* mesh, const double* prim0, const swe_param
   std::string why;
   swe_status st = check_params(&p, &why);
   if (st != SWE_OK) return fail(nullptr, st, why);
-  std::vector<HostInstance> inst(1);
-  st = read_instance(mesh, &p, &inst[0], &why);
+  HostInstance h;
+  st = read_instance(mesh, &p, &h, &why);
   if (st != SWE_OK) return fail(nullptr, st, why);
-  std::unique_ptr<swe_ctx> ctx(new swe_ctx());
-  ctx->flux = p.flux;
-  ctx->ws = p.wavespeed;
-  ctx->cfl = p.cfl;
-  int ist = 0;
-  const int64_t C = inst[0].C;
-  std::string e = ctx->eng.init(std::move(inst), p.flux, p.wavespeed, p.block, &ist, false);
-  if (!e.empty()) return fail(nullptr, (swe_status)ist, e);
-  st = upload_prim(ctx->eng, prim0, 0, C, &why);
-  if (st != SWE_OK) return fail(nullptr, st, why);
-  st = prime(ctx->eng, &why);
+  std::unique_ptr<swe_ctx> ctx;
+  if (p.reorder == SWE_REORDER_AUTO && h.C >= kTimedLayoutCells) {
+    why = swe::validate_instance(h);
+    if (!why.empty()) return fail(nullptr, SWE_ERR_INVALID_MESH, why);
+    st = create_timed(h, p, prim0, &ctx, &why);
+  } else {
+    swe::Layout L;
+    st = lay_out(&h, p.reorder, &L, &why);
+    if (st == SWE_OK) st = build_ctx(std::move(h), std::move(L), p, prim0, &ctx, &why);
+  }
   if (st != SWE_OK) return fail(nullptr, st, why);
   *out = ctx.release();
   return SWE_OK;
@@ -342,7 +493,7 @@ swe_status swe_get_prim_device(swe_ctx* ctx, double* out) {
   if (!ctx || !out) return SWE_ERR_INVALID_ARGUMENT;
   Engine& g = ctx->eng;
   const int n = g.C();
-  k_pack<<<(n + 255) / 256, 256, 0, g.stream()>>>(g.state(0, 0), g.state(0, 1), g.state(0, 2), out, n);
+  k_pack<<<(n + 255) / 256, 256, 0, g.stream()>>>(g.state(0, 0), g.state(0, 1), g.state(0, 2), out, n, g.d_cell_from);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(&ctx->err, e, "swe_get_prim_device");
   return SWE_OK;
@@ -352,7 +503,8 @@ swe_status swe_set_prim_device(swe_ctx* ctx, const double* in) {
   if (!ctx || !in) return SWE_ERR_INVALID_ARGUMENT;
   Engine& g = ctx->eng;
   const int n = g.C();
-  k_unpack<<<(n + 255) / 256, 256, 0, g.stream()>>>(in, g.state(0, 0), g.state(0, 1), g.state(0, 2), n, nullptr);
+  k_unpack<<<(n + 255) / 256, 256, 0, g.stream()>>>(in, g.state(0, 0), g.state(0, 1), g.state(0, 2), n, nullptr,
+                                                     g.d_cell_from);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(&ctx->err, e, "swe_set_prim_device");
   return SWE_OK;
@@ -373,12 +525,19 @@ swe_status swe_get_edge_values(swe_ctx* ctx, double* edg_out, double* src_out) {
   if (e == cudaSuccess) e = cudaMemcpy(sy.data(), w.sy, 3 * C * sizeof(double), cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) return cuda_fail(&ctx->err, e, "swe_get_edge_values");
   const HostInstance& h = g.host[0];
+  const swe::Layout& L = g.layouts[0];
   if (edg_out) std::memset(edg_out, 0, 6 * E * sizeof(double));
   if (src_out) std::memset(src_out, 0, 6 * E * sizeof(double));
   for (int64_t i = 0; i < C; ++i)
     for (int k = 0; k < 3; ++k) {
-      const int64_t ed = h.ce[3 * i + k], nb = h.ct[3 * i + k];
-      const int64_t id = 2 * ed + (i < nb ? 1 : 0);  // EdgeIndexer::Id (include/ValueField.h:70-75)
+      // the slot's edge, cell and neighbour in the caller's numbering
+      int64_t ed = h.ce[3 * i + k], nb = h.ct[3 * i + k], ci = i;
+      if (!L.identity()) {
+        ed = L.edge_from[ed];
+        nb = nb >= 0 ? L.cell_from[nb] : nb;
+        ci = L.cell_from[i];
+      }
+      const int64_t id = 2 * ed + (ci < nb ? 1 : 0);  // EdgeIndexer::Id (include/ValueField.h:70-75)
       const int64_t s = k * C + i;
       if (edg_out) {
         edg_out[3 * id] = ew[s];
@@ -405,10 +564,12 @@ swe_status swe_get_fluxes(swe_ctx* ctx, double* f_out) {
   if (e == cudaSuccess) e = cudaMemcpy(b.data(), g.work().f1, E * sizeof(double), cudaMemcpyDeviceToHost);
   if (e == cudaSuccess) e = cudaMemcpy(c.data(), g.work().f2, E * sizeof(double), cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) return cuda_fail(&ctx->err, e, "swe_get_fluxes");
+  const swe::Layout& L = g.layouts[0];
   for (int64_t q = 0; q < E; ++q) {
-    f_out[3 * q] = a[q];
-    f_out[3 * q + 1] = b[q];
-    f_out[3 * q + 2] = c[q];
+    const int64_t d = L.identity() ? q : L.edge_from[q];
+    f_out[3 * d] = a[q];
+    f_out[3 * d + 1] = b[q];
+    f_out[3 * d + 2] = c[q];
   }
   return SWE_OK;
   SWE_GUARD_END(&ctx->err)
@@ -423,7 +584,9 @@ swe_status swe_get_node_max(swe_ctx* ctx, double* max_out) {
   cudaError_t e = cudaStreamSynchronize(g.stream());
   if (e == cudaSuccess) e = cudaMemcpy(k.data(), g.work().maxwp, N * sizeof(k[0]), cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) return cuda_fail(&ctx->err, e, "swe_get_node_max");
-  for (int64_t q = 0; q < N; ++q) max_out[q] = swe::order_val(k[q]);
+  std::vector<double> v(N);
+  for (int64_t q = 0; q < N; ++q) v[q] = swe::order_val(k[q]);
+  nodes_to_caller(g, v.data(), max_out);
   return SWE_OK;
   SWE_GUARD_END(&ctx->err)
 }
@@ -476,7 +639,7 @@ swe_status swe_adjoint_forward(swe_ctx* ctx, int32_t scheme, int64_t n_steps, in
   for (int q = 0; q < n_gauges; ++q) {
     if (gauge_cells[q] < 0 || gauge_cells[q] >= ctx->eng.C())
       return fail(&ctx->err, SWE_ERR_INVALID_ARGUMENT, "gauge cell out of range");
-    g[q] = (int)gauge_cells[q];
+    g[q] = (int)device_cell(ctx->eng, gauge_cells[q]);
   }
   std::string e = ctx->eng.adjoint_forward(scheme, n_steps, checkpoint_every, g.data(), n_gauges, obs_every,
                                            traces_out);
@@ -488,7 +651,7 @@ swe_status swe_adjoint_forward(swe_ctx* ctx, int32_t scheme, int64_t n_steps, in
 swe_status swe_adjoint_backward(swe_ctx* ctx, const double* trace_grads, double* grad_prim0, double* grad_bathymetry) {
   if (!ctx || !grad_prim0 || !grad_bathymetry) return SWE_ERR_INVALID_ARGUMENT;
   SWE_GUARD_BEGIN
-  std::string e = ctx->eng.adjoint_backward(trace_grads, grad_prim0, grad_bathymetry);
+  std::string e = adjoint_backward_caller(ctx->eng, trace_grads, grad_prim0, grad_bathymetry);
   if (!e.empty()) return fail(&ctx->err, SWE_ERR_INVALID_ARGUMENT, e);
   return SWE_OK;
   SWE_GUARD_END(&ctx->err)
@@ -501,6 +664,48 @@ swe_status swe_adjoint_dts(swe_ctx* ctx, double* dts_out) {
   return SWE_OK;
 }
 
+swe_status swe_get_tuning(swe_ctx* ctx, int32_t* out4) {
+  if (!ctx || !out4) return SWE_ERR_INVALID_ARGUMENT;
+  out4[0] = ctx->eng.layouts.empty() ? 0 : ctx->eng.layouts[0].strategy;
+  for (int q = 0; q < 3; ++q) out4[1 + q] = ctx->eng.blocks()[q];
+  return SWE_OK;
+}
+
+swe_status swe_layout_plan(const swe_mesh* mesh, int32_t strategy, int64_t* cell_from, int64_t* edge_from,
+                           int64_t* node_from, double* cost3, int32_t* chosen) {
+  SWE_GUARD_BEGIN
+  if (strategy < SWE_REORDER_AUTO || strategy > SWE_REORDER_RCM)
+    return fail(nullptr, SWE_ERR_INVALID_ARGUMENT, "unknown reorder strategy");
+  swe_params p;
+  swe_params_default(&p);
+  HostInstance h;
+  std::string why;
+  swe_status st = read_instance(mesh, &p, &h, &why);
+  if (st != SWE_OK) return fail(nullptr, st, why);
+  why = swe::validate_instance(h);
+  if (!why.empty()) return fail(nullptr, SWE_ERR_INVALID_MESH, why);
+  double c3[3] = {0., 0., 0.};
+  swe::Layout L;
+  if (strategy == SWE_REORDER_AUTO) {
+    L = swe::choose_layout(h, strategy, c3, nullptr);
+  } else {
+    L = swe::make_layout(h, strategy);
+    c3[strategy] = swe::gather_sectors(swe::apply_layout(h, L));
+  }
+  if (cost3)
+    for (int q = 0; q < 3; ++q) cost3[q] = c3[q];
+  if (chosen) *chosen = L.strategy;
+  auto emit = [&](int64_t* out, const std::vector<int64_t>& from, int64_t n) {
+    if (!out) return;
+    for (int64_t j = 0; j < n; ++j) out[j] = L.identity() ? j : from[j];
+  };
+  emit(cell_from, L.cell_from, h.C);
+  emit(edge_from, L.edge_from, h.E);
+  emit(node_from, L.node_from, h.N);
+  return SWE_OK;
+  SWE_GUARD_END(nullptr)
+}
+
 // ------------------------------------------------------------------ batched
 swe_status swe_batch_create(int32_t n_instances, const swe_mesh* meshes, const double* const* prim0,
                             const swe_params* params, int32_t n_params, swe_batch** out) {
@@ -511,6 +716,7 @@ swe_status swe_batch_create(int32_t n_instances, const swe_mesh* meshes, const d
   if (params && n_params != 1 && n_params != n_instances)
     return fail(nullptr, SWE_ERR_INVALID_ARGUMENT, "n_params must be 1 or n_instances");
   std::vector<HostInstance> inst(n_instances);
+  std::vector<swe::Layout> lay(n_instances);
   swe_params p0;
   swe_params_default(&p0);
   if (params) p0 = params[0];
@@ -524,18 +730,22 @@ swe_status swe_batch_create(int32_t n_instances, const swe_mesh* meshes, const d
       return fail(nullptr, SWE_ERR_UNSUPPORTED, "all instances of a batch must use the same flux and wave speed");
     if (!prim0[q]) return fail(nullptr, SWE_ERR_INVALID_ARGUMENT, "prim0[" + std::to_string(q) + "] is NULL");
     st = read_instance(&meshes[q], &p, &inst[q], &why);
+    if (st == SWE_OK) st = lay_out(&inst[q], p.reorder, &lay[q], &why);
     if (st != SWE_OK) return fail(nullptr, st, "instance " + std::to_string(q) + ": " + why);
   }
   std::unique_ptr<swe_batch> b(new swe_batch());
   int ist = 0;
   std::string e = b->eng.init(std::move(inst), p0.flux, p0.wavespeed, p0.block, &ist, true);
   if (!e.empty()) return fail(nullptr, (swe_status)ist, e);
+  e = b->eng.set_layouts(std::move(lay));
+  if (!e.empty()) return fail(nullptr, SWE_ERR_CUDA, e);
   for (int q = 0; q < n_instances; ++q) {
     const int64_t c0 = b->eng.cell_off[q], n = b->eng.cell_off[q + 1] - c0;
     swe_status st = upload_prim(b->eng, prim0[q], c0, n, &why);
     if (st != SWE_OK) return fail(nullptr, st, "instance " + std::to_string(q) + ": " + why);
   }
   swe_status st = prime(b->eng, &why);
+  if (st == SWE_OK && p0.block == 0) st = tune(b->eng, &why);
   if (st != SWE_OK) return fail(nullptr, st, why);
   *out = b.release();
   return SWE_OK;
@@ -597,7 +807,7 @@ swe_status swe_batch_adjoint_forward(swe_batch* b, int32_t scheme, int64_t n_ste
   for (int q = 0; q < n_gauges; ++q) {
     if (gauge_cells[q] < 0 || gauge_cells[q] >= b->eng.C())
       return fail(&b->err, SWE_ERR_INVALID_ARGUMENT, "gauge cell out of range");
-    g[q] = (int)gauge_cells[q];
+    g[q] = (int)device_cell(b->eng, gauge_cells[q]);
   }
   std::string e = b->eng.adjoint_forward(scheme, n_steps, checkpoint_every, g.data(), n_gauges, obs_every,
                                          traces_out);
@@ -610,7 +820,7 @@ swe_status swe_batch_adjoint_backward(swe_batch* b, const double* trace_grads, d
                                       double* grad_bathymetry) {
   if (!b || !grad_prim0 || !grad_bathymetry) return SWE_ERR_INVALID_ARGUMENT;
   SWE_GUARD_BEGIN
-  std::string e = b->eng.adjoint_backward(trace_grads, grad_prim0, grad_bathymetry);
+  std::string e = adjoint_backward_caller(b->eng, trace_grads, grad_prim0, grad_bathymetry);
   if (!e.empty()) return fail(&b->err, SWE_ERR_INVALID_ARGUMENT, e);
   return SWE_OK;
   SWE_GUARD_END(&b->err)
@@ -631,6 +841,13 @@ swe_status swe_batch_integrals(swe_batch* b, int32_t q, double* out3) {
   if (e != cudaSuccess) return cuda_fail(&b->err, e, "swe_batch_integrals");
   return SWE_OK;
   SWE_GUARD_END(&b->err)
+}
+
+swe_status swe_batch_get_tuning(swe_batch* b, int32_t q, int32_t* out4) {
+  if (!b || !out4 || q < 0 || q >= b->eng.I()) return SWE_ERR_INVALID_ARGUMENT;
+  out4[0] = b->eng.layouts.empty() ? 0 : b->eng.layouts[q].strategy;
+  for (int k = 0; k < 3; ++k) out4[1 + k] = b->eng.blocks()[k];
+  return SWE_OK;
 }
 
 swe_status swe_batch_time(swe_batch* b, int32_t q, double* t) {

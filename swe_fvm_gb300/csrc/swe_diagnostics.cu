@@ -16,11 +16,13 @@ constexpr int kBlocks = 608;  // 4 per SM on 152 SMs
 constexpr int kThreads = 256;
 
 __global__ void __launch_bounds__(kThreads) k_integrals(DevMesh m, const double* W, const double* U, const double* V,
-                                                        int c0, int n, double* partial) {
+                                                        int c0, int n, const int* __restrict__ to, double* partial) {
   __shared__ double s[3][kThreads];
   double a0 = 0., a1 = 0., a2 = 0.;
+  // cells visited in the caller's order (to: caller's row -> device cell), so
+  // that the sums are the same in every device order
   for (int q = blockIdx.x * kThreads + threadIdx.x; q < n; q += kBlocks * kThreads) {
-    const int i = c0 + q;
+    const int i = to ? to[c0 + q] : c0 + q;
     const double b = m.bc[i];
     const double h = W[i] - b;
     if (is_wet(h)) {
@@ -59,7 +61,7 @@ cudaError_t Engine::integrals(int64_t c0, int64_t n, double* out_host) {
     if (!d_integrals_) return cudaErrorMemoryAllocation;
   }
   k_integrals<<<kBlocks, kThreads, 0, stream_>>>(mesh_, state(0, 0), state(0, 1), state(0, 2), (int)c0, (int)n,
-                                                 d_integrals_);
+                                                 d_cell_to, d_integrals_);
   k_integrals_final<<<1, 32, 0, stream_>>>(d_integrals_, d_integrals_ + 3 * kBlocks);
   launches_ += 2;
   cudaError_t e = cudaMemcpyAsync(out_host, d_integrals_ + 3 * kBlocks, 3 * sizeof(double), cudaMemcpyDeviceToHost,

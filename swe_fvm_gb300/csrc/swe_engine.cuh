@@ -127,6 +127,18 @@ struct HostInstance {
   double cfl, cor;
 };
 
+// Order of an instance's cells, edges and nodes on the device
+// (swe_layout.cuh builds them).
+enum : int { kLayoutAuto = -1, kLayoutKeep = 0, kLayoutMorton = 1, kLayoutRcm = 2 };
+struct Layout {
+  int strategy = kLayoutKeep;
+  // device position -> the caller's index (empty when strategy is kLayoutKeep)
+  std::vector<int64_t> cell_from, edge_from, node_from;
+  // the caller's cell index -> device position
+  std::vector<int64_t> cell_to;
+  bool identity() const { return strategy == kLayoutKeep; }
+};
+
 struct AdjWork;
 struct AdjointState;
 void adjoint_state_delete(AdjointState* a);
@@ -137,7 +149,36 @@ class Engine {
   ~Engine();
   // Validates and precomputes every instance, uploads, allocates work arrays.
   // Returns an empty string on success, else the error message (status in *st).
+  // block > 0 fixes the threads per block of every cell and edge kernel.
   std::string init(std::vector<HostInstance>&& inst, int flux, int ws, int block, int* st, bool batched);
+
+  // Threads per block of the reconstruction kernels (k_recon1, k_recon2), the
+  // edge-flux kernel (k_flux) and the drain/update kernels; drops the
+  // captured step graphs when they change.
+  void set_blocks(const int blocks[3]);
+  const int* blocks() const { return blk_; }
+  // Times steps of `scheme` with 64, 128 and 256 threads per block and keeps
+  // the fastest per kernel group.  The state, the accumulated time and the
+  // error word are restored; the caller re-primes the flux pass.  Choices are
+  // cached per (device, flux, wave speed, batched, Coriolis, scheme,
+  // log2 of the cell count) for the life of the process.
+  cudaError_t autotune_blocks(int scheme);
+  // Cell layouts of the instances (device position -> caller's index) and
+  // their device copies over the concatenated cells: d_cell_from (global
+  // device position -> the caller's local row) and d_cell_to (global caller
+  // row -> global device position); both null when every instance keeps the
+  // caller's order.
+  std::vector<Layout> layouts;
+  int* d_cell_from = nullptr;
+  int* d_cell_to = nullptr;
+  std::string set_layouts(std::vector<Layout>&& lay);
+  // Mean ms of one graph-replayed step of `scheme` (CFL dt) over n steps after
+  // one warm-up replay, run from the current state, which is then restored
+  // with the accumulated time, the step dt and the error word (the caller
+  // re-primes the flux pass).
+  cudaError_t time_steps(int scheme, int n, float* ms);
+  // Device bytes this engine allocated.
+  size_t device_bytes() const { return bytes_; }
 
   // NULL selects the engine's own non-blocking stream.
   void set_stream(cudaStream_t s) { stream_ = s ? s : own_stream_; }
@@ -221,10 +262,11 @@ class Engine {
   // partially-wet cells run on it while the other edges' fluxes run on stream_
   cudaStream_t side_ = nullptr;
   cudaEvent_t ev_fork_ = nullptr, ev_join_ = nullptr;
-  int flux_ = 1, ws_ = 2, block_ = 256;
+  int flux_ = 1, ws_ = 2;
+  int blk_[3] = {256, 256, 256};  // reconstruction, edge flux, drain/update
   bool batched_ = false;
-  bool cor0_ = true;
-  double* d_integrals_ = nullptr;  // partial sums of the integrals  // every instance has cor = 0: no Coriolis arithmetic in the reconstruction
+  bool cor0_ = true;  // every instance has cor = 0: no Coriolis arithmetic in the reconstruction
+  double* d_integrals_ = nullptr;  // partial sums of the integrals
   void launch_recon1(const double* W, const double* U, const double* V, int latch_mode);
   void launch_recon2(const double* W, const double* U, const double* V, cudaStream_t s);
   // fluxes: mode 0 every edge; mode 1 the edges with no partially-wet cell;
@@ -234,6 +276,10 @@ class Engine {
   void launch_update(const Stage& st, const double* const* in, const double* const* u0, double* const* out,
                      double* nst);
   int64_t launches_ = 0;
+  size_t bytes_ = 0;
+  // copy of the state (3 x C) to or from buf; after a restore also zeroes the
+  // accumulated time, the step dt and the error word
+  cudaError_t snapshot(double* buf, bool restore);
   cudaGraphExec_t graphs_[3][3] = {};
   AdjointState* adj_ = nullptr;
 };

@@ -1,14 +1,16 @@
 // swe_kernels.cu -- sm_103a kernels of one Runge-Kutta stage and the engine
 // that sequences them.
 //
-// A stage (src/Solvers.cpp:5-59) is five kernels over the concatenated cells
+// A stage (src/Solvers.cpp:5-59) is six kernels over the concatenated cells
 // and edges of every instance:
 //   k_recon1  all cells    SpaceDisc::ComputeInterfaceValues pass 1
 //                          (src/SpaceDisc.cpp:37-45) + node maxima
 //   k_recon2  part-wet     pass 2 (src/SpaceDisc.cpp:47-51), reading the
 //                          pass-1 node maxima only (order-independent)
 //   k_flux    all edges    SpaceDisc::ComputeFluxes (src/SpaceDisc.cpp:54-74)
-//                          with the flux plugin and the CFL min-reduction
+//                          with the flux plugin and the CFL min-reduction,
+//                          except the edges of partially-wet cells
+//   k_flux_pw those edges  on a second stream, after k_recon2
 //   k_drain   all cells    TimeDisc::ComputeDrainingDt (src/TimeDisc.cpp:43-66),
 //                          once per cell instead of 4x per RHS
 //   k_update  all cells    TimeDisc::RHS + ConsAssigner (src/TimeDisc.cpp:3-41,
@@ -18,9 +20,13 @@
 // CFL minimum, part-wet list append) are exact max/min/append operations.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <array>
 #include <cstdio>
 #include <cstring>
 #include <limits>
+#include <map>
+#include <mutex>
 #include <string>
 
 #include "swe_engine.cuh"
@@ -556,6 +562,7 @@ T* Engine::dalloc(size_t n) {
   if (n == 0) n = 1;
   if (cudaMalloc(&p, n * sizeof(T)) != cudaSuccess) return nullptr;
   allocs_.push_back(p);
+  bytes_ += n * sizeof(T);
   return (T*)p;
 }
 
@@ -576,8 +583,7 @@ std::string Engine::init(std::vector<HostInstance>&& inst, int flux, int ws, int
   *st = 0;
   flux_ = flux;
   ws_ = ws;
-  block_ = 256;
-  (void)block;
+  if (block > 0) blk_[0] = blk_[1] = blk_[2] = block;
   batched_ = batched;
   const int I = (int)inst.size();
   int64_t C = 0, E = 0, N = 0;
@@ -715,7 +721,7 @@ cudaError_t Engine::reset_pass() {
 }
 
 void Engine::launch_recon1(const double* W, const double* U, const double* V, int latch_mode) {
-  const int b = block_, g = nblocks(mesh_.C, b);
+  const int b = blk_[0], g = nblocks(mesh_.C, b);
   if (batched_) {
     if (cor0_) k_recon1<true, true><<<g, b, 0, stream_>>>(mesh_, work_, W, U, V, latch_mode);
     else k_recon1<true, false><<<g, b, 0, stream_>>>(mesh_, work_, W, U, V, latch_mode);
@@ -727,7 +733,7 @@ void Engine::launch_recon1(const double* W, const double* U, const double* V, in
 }
 
 void Engine::launch_recon2(const double* W, const double* U, const double* V, cudaStream_t s) {
-  const int b = block_, g = std::max(1, std::min(nblocks(mesh_.C, b), 152 * 8));
+  const int b = blk_[0], g = std::max(1, std::min(nblocks(mesh_.C, b), 152 * 2048 / b));
   if (batched_) {
     if (cor0_) k_recon2<true, true><<<g, b, 0, s>>>(mesh_, work_, W, U, V);
     else k_recon2<true, false><<<g, b, 0, s>>>(mesh_, work_, W, U, V);
@@ -739,7 +745,6 @@ void Engine::launch_recon2(const double* W, const double* U, const double* V, cu
 }
 
 cudaError_t Engine::interface_values(const double* W, const double* U, const double* V, int latch_mode) {
-  const int b = block_;
   launch_recon1(W, U, V, latch_mode);
   launch_recon2(W, U, V, stream_);
   return cudaGetLastError();
@@ -777,7 +782,7 @@ static void launch_flux_pw(bool batched, int blocks, cudaStream_t s, const DevMe
 cudaError_t Engine::fluxes(const double* W) { return fluxes(W, 0); }
 
 cudaError_t Engine::fluxes(const double* W, int mode) {
-  const int b = block_, g = nblocks(mesh_.E, b);
+  const int b = blk_[1], g = nblocks(mesh_.E, b);
   switch (flux_ * 3 + ws_) {
     case 0: launch_flux<HLL<Rusanov>>(batched_, mode, g, b, stream_, mesh_, work_, W); break;
     case 1: launch_flux<HLL<Davis>>(batched_, mode, g, b, stream_, mesh_, work_, W); break;
@@ -805,7 +810,7 @@ void Engine::fluxes_pw(const double* W, cudaStream_t s) {
 
 cudaError_t Engine::launch_stage(const Stage& st, const double* const* in, const double* const* u0,
                                  double* const* out, bool first_stage_of_step, int latch_mode, cudaEvent_t* ev) {
-  const int b = block_;
+  const int b = blk_[2];
   const int lm = first_stage_of_step ? latch_mode : 0;
   if (ev) cudaEventRecord(ev[0], stream_);
   launch_recon1(in[0], in[1], in[2], lm);
@@ -846,7 +851,7 @@ static void update_kernel(int g, int b, cudaStream_t s, const DevMesh& m, const 
 
 void Engine::launch_update(const Stage& st, const double* const* in, const double* const* u0, double* const* out,
                            double* nst) {
-  const int b = block_, g = nblocks(mesh_.C, b);
+  const int b = blk_[2], g = nblocks(mesh_.C, b);
   const bool half = !st.first && st.a == 0.5 && st.b == 0.5 && st.c == 0.5;
   const int sel = (batched_ ? 4 : 0) | (nst ? 2 : 0) | (half ? 1 : 0);
   switch (sel) {
@@ -891,6 +896,143 @@ cudaError_t Engine::step_timed(int scheme, int latch_mode, double* acc) {
   for (auto& row : ev)
     for (auto& x : row) cudaEventDestroy(x);
   return e;
+}
+
+void Engine::set_blocks(const int blocks[3]) {
+  bool same = true;
+  for (int q = 0; q < 3; ++q) same = same && blk_[q] == blocks[q];
+  if (same) return;
+  for (int q = 0; q < 3; ++q) blk_[q] = blocks[q];
+  for (auto& row : graphs_)
+    for (auto& g : row)
+      if (g) {
+        cudaGraphExecDestroy(g);
+        g = nullptr;
+      }
+}
+
+namespace {
+std::mutex g_tune_mu;
+std::map<std::array<int, 7>, std::array<int, 3>> g_tune_cache;
+}  // namespace
+
+cudaError_t Engine::snapshot(double* buf, bool restore) {
+  const int64_t C = mesh_.C;
+  cudaError_t r = cudaSuccess;
+  for (int c = 0; c < 3 && r == cudaSuccess; ++c)
+    r = restore ? cudaMemcpyAsync(state(0, c), buf + c * C, C * sizeof(double), cudaMemcpyDeviceToDevice, stream_)
+                : cudaMemcpyAsync(buf + c * C, state(0, c), C * sizeof(double), cudaMemcpyDeviceToDevice, stream_);
+  if (restore) {
+    if (r == cudaSuccess) r = cudaMemsetAsync(work_.tsum, 0, mesh_.I * sizeof(double), stream_);
+    if (r == cudaSuccess) r = cudaMemsetAsync(work_.dt, 0, mesh_.I * sizeof(double), stream_);
+    if (r == cudaSuccess) r = cudaMemsetAsync(work_.err, 0, sizeof(unsigned), stream_);
+  }
+  return r;
+}
+
+cudaError_t Engine::autotune_blocks(int scheme) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  int lg = 0;
+  while ((1ll << (lg + 1)) <= (int64_t)mesh_.C) ++lg;
+  const std::array<int, 7> key = {dev, flux_, ws_, batched_ ? 1 : 0, cor0_ ? 1 : 0, scheme, lg};
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune_cache.find(key);
+    if (it != g_tune_cache.end()) {
+      set_blocks(it->second.data());
+      return cudaSuccess;
+    }
+  }
+  double* save = nullptr;
+  e = cudaMalloc(&save, 3 * (size_t)mesh_.C * sizeof(double));
+  if (e != cudaSuccess) return e;
+  static const int kCand[3] = {64, 128, 256};
+  const double inf = std::numeric_limits<double>::infinity();
+  double t[3][3] = {{inf, inf, inf}, {inf, inf, inf}, {inf, inf, inf}};  // [group][candidate]
+  e = snapshot(save, false);
+  for (int ci = 0; ci < 3 && e == cudaSuccess; ++ci) {
+    const int b3[3] = {kCand[ci], kCand[ci], kCand[ci]};
+    set_blocks(b3);
+    for (int rep = 0; rep < 4 && e == cudaSuccess; ++rep) {  // rep 0 warms up
+      double acc[6] = {0., 0., 0., 0., 0., 0.};
+      e = snapshot(save, true);
+      if (e == cudaSuccess) e = step_timed(scheme, 1, acc);
+      if (e != cudaSuccess || rep == 0) continue;
+      t[0][ci] = std::min(t[0][ci], acc[0] + acc[1]);
+      t[1][ci] = std::min(t[1][ci], acc[2]);
+      t[2][ci] = std::min(t[2][ci], acc[3] + acc[4]);
+    }
+  }
+  int best[3] = {256, 256, 256};
+  if (e == cudaSuccess)
+    for (int g = 0; g < 3; ++g) {
+      int k = 2;  // ties keep the largest block
+      for (int ci = 1; ci >= 0; --ci)
+        if (t[g][ci] < t[g][k]) k = ci;
+      best[g] = kCand[k];
+    }
+  set_blocks(best);
+  // back to the state before tuning
+  cudaError_t e2 = snapshot(save, true);
+  if (e2 == cudaSuccess) e2 = cudaStreamSynchronize(stream_);
+  cudaFree(save);
+  if (e == cudaSuccess) e = e2;
+  if (e == cudaSuccess) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune_cache[key] = {best[0], best[1], best[2]};
+  }
+  return e;
+}
+
+cudaError_t Engine::time_steps(int scheme, int n, float* ms) {
+  double* save = nullptr;
+  cudaError_t e = cudaMalloc(&save, 3 * (size_t)mesh_.C * sizeof(double));
+  if (e != cudaSuccess) return e;
+  cudaEvent_t a = nullptr, b = nullptr;
+  e = snapshot(save, false);
+  if (e == cudaSuccess) e = cudaEventCreate(&a);
+  if (e == cudaSuccess) e = cudaEventCreate(&b);
+  if (e == cudaSuccess) e = run_graph(scheme, 1, 1);
+  if (e == cudaSuccess) e = cudaEventRecord(a, stream_);
+  if (e == cudaSuccess) e = run_graph(scheme, 1, n);
+  if (e == cudaSuccess) e = cudaEventRecord(b, stream_);
+  if (e == cudaSuccess) e = cudaEventSynchronize(b);
+  if (e == cudaSuccess) {
+    e = cudaEventElapsedTime(ms, a, b);
+    *ms /= (float)n;
+  }
+  cudaError_t e2 = snapshot(save, true);
+  if (e2 == cudaSuccess) e2 = cudaStreamSynchronize(stream_);
+  if (a) cudaEventDestroy(a);
+  if (b) cudaEventDestroy(b);
+  cudaFree(save);
+  return e == cudaSuccess ? e2 : e;
+}
+
+std::string Engine::set_layouts(std::vector<Layout>&& lay) {
+  layouts = std::move(lay);
+  bool any = false;
+  for (const Layout& L : layouts) any = any || !L.identity();
+  if (!any) return "";
+  std::vector<int> from((size_t)mesh_.C);
+  for (size_t q = 0; q < layouts.size(); ++q) {
+    const int64_t c0 = cell_off[q], n = cell_off[q + 1] - c0;
+    for (int64_t j = 0; j < n; ++j) from[c0 + j] = layouts[q].identity() ? (int)j : (int)layouts[q].cell_from[j];
+  }
+  std::vector<int> to((size_t)mesh_.C);
+  for (size_t q = 0; q < layouts.size(); ++q) {
+    const int64_t c0 = cell_off[q], n = cell_off[q + 1] - c0;
+    for (int64_t j = 0; j < n; ++j) to[c0 + from[c0 + j]] = (int)(c0 + j);
+  }
+  d_cell_from = dalloc<int>(from.size());
+  d_cell_to = dalloc<int>(to.size());
+  if (!d_cell_from || !d_cell_to) return "device allocation failed";
+  if (cudaMemcpy(d_cell_from, from.data(), from.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(d_cell_to, to.data(), to.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess)
+    return std::string("uploading the cell layout: ") + cudaGetErrorString(cudaGetLastError());
+  return "";
 }
 
 cudaError_t Engine::update_only(const Stage& st, const double* const* in, const double* const* u0,

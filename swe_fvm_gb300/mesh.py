@@ -146,6 +146,29 @@ def reorder_morton(points_xyz: np.ndarray, triangles: np.ndarray):
     return pts, tri[cell_perm]
 
 
+def renumbered(m: Mesh, cell_from, edge_from, node_from) -> Mesh:
+    """The same mesh with cells, edges and nodes renumbered: new cell j is old
+    cell cell_from[j] (likewise edges and nodes); every cell's and edge's own
+    row order is kept, so the step computes the same values per cell."""
+    cf, ef, nf = (np.asarray(a, dtype=np.int64) for a in (cell_from, edge_from, node_from))
+    ic, ie, inn = np.empty_like(cf), np.empty_like(ef), np.empty_like(nf)
+    ic[cf], ie[ef], inn[nf] = np.arange(cf.size), np.arange(ef.size), np.arange(nf.size)
+
+    def cells(a):
+        return np.where(a >= 0, ic[np.maximum(a, 0)], a)
+
+    return Mesh(m.geometry[nf].copy(), inn[m.edge_nodes[ef]], cells(m.edge_cells[ef]), inn[m.cell_nodes[cf]],
+                ie[m.cell_edges[cf]], cells(m.cell_neighbours[cf])).contiguous()
+
+
+def shuffled(m: Mesh, seed: int):
+    """m with cells, edges and nodes numbered at random (a worst case for
+    memory locality).  Returns (mesh, cell_from, edge_from, node_from)."""
+    rng = np.random.default_rng(seed)
+    cf, ef, nf = rng.permutation(m.num_cells), rng.permutation(m.num_edges), rng.permutation(m.num_nodes)
+    return renumbered(m, cf, ef, nf), cf, ef, nf
+
+
 def structured_square(n: int, lo: float, hi: float, bathymetry=None) -> Mesh:
     """[lo, hi]^2 split into n x n squares, 2 triangles each.
 

@@ -127,7 +127,13 @@ def _swe_mesh(m: Mesh):
     return sm, keep
 
 
-def make_params(fluxer: Fluxer, cor=0.0, tau=0.0, cfl=0.15) -> SweParams:
+REORDER = {"auto": -1, "keep": 0, "morton": 1, "rcm": 2}
+
+
+def make_params(fluxer: Fluxer, cor=0.0, tau=0.0, cfl=0.15, reorder="auto", block=0) -> SweParams:
+    """swe_params for a flux plugin; ``reorder`` is one of REORDER's keys (the
+    device order of cells, edges and nodes), ``block`` the threads per block
+    (0: timed at creation)."""
     L = _lib.load()
     p = SweParams()
     L.swe_params_default(ctypes.byref(p))
@@ -136,7 +142,35 @@ def make_params(fluxer: Fluxer, cor=0.0, tau=0.0, cfl=0.15) -> SweParams:
     p.cor = float(cor)
     p.tau = float(tau)
     p.cfl = float(cfl)
+    p.reorder = REORDER[reorder] if isinstance(reorder, str) else int(reorder)
+    p.block = int(block)
     return p
+
+
+def _tuning(out: np.ndarray) -> dict:
+    names = {v: k for k, v in REORDER.items()}
+    return {"reorder": names.get(int(out[0]), int(out[0])), "block_recon": int(out[1]), "block_flux": int(out[2]),
+            "block_update": int(out[3])}
+
+
+def layout_plan(mesh: Mesh, reorder="auto") -> dict:
+    """The device order swe_create would use for ``mesh`` (host only, no GPU):
+    cell_from / edge_from / node_from give the mesh's index at every device
+    position, cost the gathered 32-byte sectors of keep, morton and rcm, and
+    chosen the strategy."""
+    L = _lib.load()
+    sm, keep = _swe_mesh(mesh)
+    cf = np.empty(mesh.num_cells, dtype=np.int64)
+    ef = np.empty(mesh.num_edges, dtype=np.int64)
+    nf = np.empty(mesh.num_nodes, dtype=np.int64)
+    cost = np.zeros(3)
+    chosen = ctypes.c_int32()
+    code = REORDER[reorder] if isinstance(reorder, str) else int(reorder)
+    st = L.swe_layout_plan(ctypes.byref(sm), code, cf.ctypes.data, ef.ctypes.data, nf.ctypes.data, cost.ctypes.data,
+                           ctypes.byref(chosen))
+    check(st, None)
+    names = {v: k for k, v in REORDER.items()}
+    return {"cell_from": cf, "edge_from": ef, "node_from": nf, "cost": cost, "chosen": names[chosen.value]}
 
 
 class SpaceDisc:
@@ -146,7 +180,8 @@ class SpaceDisc:
     arrays are copied to the current CUDA device.
     """
 
-    def __init__(self, fluxer: Fluxer, domain, v0, cor: float = 0.0, tau: float = 0.0, cfl: float = 0.15):
+    def __init__(self, fluxer: Fluxer, domain, v0, cor: float = 0.0, tau: float = 0.0, cfl: float = 0.15,
+                 reorder="auto", block: int = 0):
         L = _lib.load()
         if isinstance(domain, Mesh):
             domain = Domain.from_mesh(domain)
@@ -156,7 +191,7 @@ class SpaceDisc:
         m = domain.mesh()
         sm, self._keep = _swe_mesh(m)
         prim = np.ascontiguousarray(v0, dtype=np.float64).reshape(m.num_cells, 3)
-        p = make_params(fluxer, cor, tau, cfl)
+        p = make_params(fluxer, cor, tau, cfl, reorder, block)
         ctx = ctypes.c_void_p()
         st = L.swe_create(ctypes.byref(sm), prim.ctypes.data, ctypes.byref(p), ctypes.byref(ctx))
         check(st, None)
@@ -258,6 +293,12 @@ class SpaceDisc:
         self._check(_lib.load().swe_launch_count(self.ctx, ctypes.byref(n)))
         return n.value
 
+    def tuning(self) -> dict:
+        """The device order and the threads per block the context runs with."""
+        out = np.zeros(4, dtype=np.int32)
+        self._check(_lib.load().swe_get_tuning(self.ctx, out.ctypes.data))
+        return _tuning(out)
+
     def get_prim_device(self, ptr: int) -> None:
         self._check(_lib.load().swe_get_prim_device(self.ctx, ctypes.c_void_p(ptr)))
 
@@ -316,7 +357,7 @@ class Batch:
     """Many independent instances stepped together (one launch per stage
     kernel over all instances, each with its own CFL time step)."""
 
-    def __init__(self, meshes, prims, fluxer: Fluxer = None, cor=0.0, cfl=0.15):
+    def __init__(self, meshes, prims, fluxer: Fluxer = None, cor=0.0, cfl=0.15, reorder="auto", block: int = 0):
         L = _lib.load()
         fluxer = fluxer or Fluxes.HLLC(Wavespeeds.Einfeldt)
         n = len(meshes)
@@ -331,7 +372,7 @@ class Batch:
             pp = np.ascontiguousarray(p, dtype=np.float64).reshape(m.num_cells, 3)
             self._keep.append((keep, pp))
             ptrs[q] = pp.ctypes.data
-        params = make_params(fluxer, cor, 0.0, cfl)
+        params = make_params(fluxer, cor, 0.0, cfl, reorder, block)
         b = ctypes.c_void_p()
         st = L.swe_batch_create(n, arr, ptrs, ctypes.byref(params), 1, ctypes.byref(b))
         check(st, None, batch=True)
@@ -383,6 +424,12 @@ class Batch:
         self._check(_lib.load().swe_batch_launch_count(self.b, ctypes.byref(n)))
         return n.value
 
+    def tuning(self, q: int = 0) -> dict:
+        """Device order of instance q and the batch's threads per block."""
+        out = np.zeros(4, dtype=np.int32)
+        self._check(_lib.load().swe_batch_get_tuning(self.b, int(q), out.ctypes.data))
+        return _tuning(out)
+
 
 __all__ = ["Topology", "Domain", "Wavespeeds", "Fluxes", "Fluxer", "SpaceDisc", "TimeDisc", "Solvers", "Batch",
-           "SweError", "SCHEMES"]
+           "SweError", "SCHEMES", "REORDER", "layout_plan"]

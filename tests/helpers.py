@@ -16,3 +16,13 @@ def max_abs(a, b) -> float:
 def cons(prim, bc):
     h = prim[:, 0] - bc
     return np.stack([h, h * prim[:, 1], h * prim[:, 2]], axis=1)
+
+
+
+def shuffle_mesh(m, seed):
+    """The same mesh with its cells, edges and nodes renumbered at random
+    (each cell's and edge's own row order kept).  Returns (mesh, pc, pe, pn),
+    p*[new] = old index."""
+    from swe_fvm_gb300.mesh import shuffled
+
+    return shuffled(m, seed)

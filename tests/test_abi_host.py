@@ -44,6 +44,7 @@ def test_params_default_are_the_reference_values():
     p = _lib.SweParams()
     assert L.swe_params_default(ctypes.byref(p)) == 0
     assert (p.flux, p.wavespeed, p.cor, p.tau, p.cfl) == (1, 2, 0.0, 0.0, 0.15)
+    assert (p.reorder, p.block) == (-1, 0)  # device order and block sizes tuned
 
 
 def _create(m, prim, fluxer=None):
