@@ -188,14 +188,17 @@ def run_gpu(args):
         gauges = np.random.default_rng(11).choice(am.num_cells, 64, replace=False)
         ps = SpaceDisc(Fluxes.HLLC(Wavespeeds.Einfeldt), am, ap)
         ps.set_stream(stream.cuda_stream)
+        ro = Rollout(am, ap)
+        torch.cuda.synchronize()
+        # the profiled range (ncu --profile-from-start off): creation and
+        # tuning stay outside it
+        torch.cuda.cudart().cudaProfilerStart()
         ps.run_cfl(1, 2)
         ps.synchronize()
         t0 = time.perf_counter()
         ps.run_cfl(1, args.steps)
         ps.synchronize()
         t_plain = time.perf_counter() - t0
-        del ps
-        ro = Rollout(am, ap)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         tr = ro.forward(1, args.steps, 50, gauges, 10)
@@ -203,15 +206,20 @@ def run_gpu(args):
         t0 = time.perf_counter()
         ro.backward(np.ones_like(tr))
         t_bwd = time.perf_counter() - t0
+        torch.cuda.cudart().cudaProfilerStop()
         print(json.dumps({"adjoint_profile": True, "cells": am.num_cells, "steps": args.steps,
                           "plain_s": t_plain, "taped_forward_s": t_fwd, "backward_s": t_bwd,
                           "ratio": (t_fwd + t_bwd) / t_plain}))
         return
     if args.profile:
-        # profiling driver: warm-up, then exactly K graph-replayed steps
+        # profiling driver: warm-up, then exactly K graph-replayed steps inside
+        # the profiled range (ncu --profile-from-start off)
         sd.run_cfl(1, args.warmup)
+        sd.synchronize()
+        torch.cuda.cudart().cudaProfilerStart()
         sd.run_cfl(1, args.steps)
         sd.synchronize()
+        torch.cuda.cudart().cudaProfilerStop()
         print(json.dumps({"profile": True, "cells": C, "steps": args.steps, "warmup": args.warmup}))
         return
     # warm-up (graph capture happens on the first replay)
