@@ -69,7 +69,12 @@ typedef enum swe_reorder {
   SWE_REORDER_RCM = 2
 } swe_reorder;
 /* Time scheme: Solvers::Euler / SSPRK2 / SSPRK3 (src/Solvers.cpp:5-59). */
-typedef enum swe_scheme { SWE_SCHEME_EULER = 0, SWE_SCHEME_SSPRK2 = 1, SWE_SCHEME_SSPRK3 = 2 } swe_scheme;
+typedef enum swe_scheme {
+  SWE_SCHEME_EULER = 0,
+  SWE_SCHEME_SSPRK2 = 1,
+  SWE_SCHEME_SSPRK3 = 2,
+  SWE_SCHEME_CUSTOM = 3 /* the table given to swe_set_scheme */
+} swe_scheme;
 
 /* Mesh in the reference's arrays (Topology + Domain geometry). */
 typedef struct swe_mesh {
@@ -198,6 +203,17 @@ swe_status swe_synchronize(swe_ctx* ctx);
  * on this thread).  Never NULL. */
 const char* swe_last_error(swe_ctx* ctx);
 
+/* Time-scheme plugin: defines SWE_SCHEME_CUSTOM as a Shu-Osher table of
+ * n_stages (1 to 4) stages, the form the reference's Solvers are written in
+ * (src/Solvers.cpp:5-59): U_s = a[s] U0 + b[s] U_{s-1} + RHS(U_{s-1}, c[s] dt)
+ * with U_{-1} = U0, each stage written through ConsAssigner; a[s] + b[s] = 1
+ * and c[s] > 0.  Euler is {1}, {0}, {1}; SSPRK2 {1, 0.5}, {0, 0.5}, {1, 0.5};
+ * SSPRK3 {1, 0.75, 1/3}, {0, 0.25, 2/3}, {1, 0.25, 2/3}.  Every entry point
+ * that takes a scheme (steps, CFL runs, kernel timing, the adjoint) then
+ * accepts SWE_SCHEME_CUSTOM; redefining it replaces the table for later calls
+ * (a taped adjoint run keeps the table it ran with). */
+swe_status swe_set_scheme(swe_ctx* ctx, int32_t n_stages, const double* a, const double* b, const double* c);
+
 /* What the tuner chose: out4 = {device order (swe_reorder), threads per block
  * of the reconstruction kernels, of the edge-flux kernel, of the drain and
  * update kernels}.  Block sizes are timed at creation when swe_params.block
@@ -281,6 +297,8 @@ swe_status swe_batch_get_prim(swe_batch* b, int32_t instance, double* prim_out);
 /* Sum of the dts taken by an instance so far. */
 swe_status swe_batch_time(swe_batch* b, int32_t instance, double* t);
 swe_status swe_batch_launch_count(swe_batch* b, int64_t* n);
+/* swe_set_scheme for every instance of a batch. */
+swe_status swe_batch_set_scheme(swe_batch* bt, int32_t n_stages, const double* a, const double* b, const double* c);
 /* swe_get_tuning for instance q of a batch (block sizes are shared). */
 swe_status swe_batch_get_tuning(swe_batch* b, int32_t q, int32_t* out4);
 swe_status swe_batch_synchronize(swe_batch* b);

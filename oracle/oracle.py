@@ -48,6 +48,7 @@ def lib():
         L.oracle_create.argtypes = [i64, i64, i64, vp, vp, vp, vp, vp, vp, vp, i32, i32, d, d, i32]
         L.oracle_destroy.argtypes = [vp]
         L.oracle_step.argtypes = [vp, i32, d]
+        L.oracle_step_table.argtypes = [vp, i32, vp, vp, vp, d]
         L.oracle_compute_interface_values.argtypes = [vp]
         L.oracle_compute_fluxes.argtypes = [vp]
         L.oracle_min_len_to_wavespeed.argtypes = [vp]
@@ -93,6 +94,12 @@ class Oracle:
 
     def step(self, scheme="SSPRK2", dt=1e-3):
         lib().oracle_step(self.ptr, SCHEME[scheme], float(dt))
+
+    def step_table(self, a, b, c, dt):
+        """One step of a Shu-Osher table (stage s: a[s] U0 + b[s] U_{s-1} +
+        RHS(U_{s-1}, c[s] dt))."""
+        a, b, c = (np.ascontiguousarray(x, dtype=np.float64) for x in (a, b, c))
+        lib().oracle_step_table(self.ptr, len(a), _p(a), _p(b), _p(c), float(dt))
 
     def compute_interface_values(self):
         lib().oracle_compute_interface_values(self.ptr)

@@ -865,6 +865,24 @@ void oracle_step(oracle_ctx* c, int scheme, double dt) {
   free(u0);
 }
 
+/* A caller's Shu-Osher table: stage s is U_s = a[s] U0 + b[s] U_{s-1} +
+ * RHS(U_{s-1}, cc[s] dt) with U_{-1} = U0; stage 0 with c = 1 and (a, b) =
+ * (1, 0) or (0, 1) is the plain U0 + RHS(dt) of the built-in schemes'
+ * first stage (the same rule as the GPU library's swe_set_scheme). */
+void oracle_step_table(oracle_ctx* c, int n, const double* a, const double* b, const double* cc, double dt) {
+  const int64_t C = c->m.num_cells;
+  double* u0 = (double*)malloc((size_t)C * 3 * sizeof(double));
+  memcpy(u0, c->vol, (size_t)C * 3 * sizeof(double));
+  for (int s = 0; s < n; ++s) {
+    const int first = s == 0 && cc[s] == 1. && ((a[s] == 1. && b[s] == 0.) || (a[s] == 0. && b[s] == 1.));
+    if (first)
+      rk_stage(c, u0, 1, 0., 0., dt);
+    else
+      rk_stage(c, u0, 0, a[s], b[s], cc[s] * dt);
+  }
+  free(u0);
+}
+
 /* include/TimeDisc.h:13,22 with the coefficient as a parameter */
 double oracle_min_len_to_wavespeed(const oracle_ctx* c) { return c->r; }
 

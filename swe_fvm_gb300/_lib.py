@@ -34,6 +34,7 @@ EXPORTS = [
     "swe_batch_get_prim", "swe_batch_time", "swe_batch_launch_count", "swe_batch_synchronize",
     "swe_batch_last_error", "swe_batch_adjoint_forward", "swe_batch_adjoint_backward", "swe_batch_adjoint_dts",
     "swe_integrals", "swe_batch_integrals", "swe_get_tuning", "swe_batch_get_tuning", "swe_layout_plan",
+    "swe_set_scheme", "swe_batch_set_scheme",
 ]
 
 
@@ -135,6 +136,8 @@ def load(build_if_needed: bool = True):
         "swe_get_tuning": [vp, vp],
         "swe_batch_get_tuning": [vp, i32, vp],
         "swe_layout_plan": [vp, i32, vp, vp, vp, vp, P(i32)],
+        "swe_set_scheme": [vp, i32, vp, vp, vp],
+        "swe_batch_set_scheme": [vp, i32, vp, vp, vp],
     }
     for name, args in sig.items():
         f = getattr(L, name)

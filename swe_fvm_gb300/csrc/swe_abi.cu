@@ -167,6 +167,28 @@ std::string adjoint_backward_caller(Engine& g, const double* trace_grads, double
 // Times the block sizes (swe_params.block == 0) and re-primes the flux pass.
 swe_status tune(Engine& eng, std::string* err);
 
+constexpr const char* kSchemeMsg = "scheme must be 0, 1, 2 or SWE_SCHEME_CUSTOM once defined";
+
+// A caller's Shu-Osher table (swe_set_scheme) as engine stages; "" or why not.
+std::string make_scheme(int32_t n, const double* a, const double* b, const double* c, swe::Scheme* out) {
+  if (n < 1 || n > swe::kMaxStages) return "n_stages must be 1 to " + std::to_string(swe::kMaxStages);
+  if (!a || !b || !c) return "a, b and c are required";
+  swe::Scheme sc{};
+  sc.n = n;
+  for (int s = 0; s < n; ++s) {
+    if (!std::isfinite(a[s]) || !std::isfinite(b[s]) || !(c[s] > 0.) || !std::isfinite(c[s]))
+      return "stage " + std::to_string(s) + ": a and b must be finite and c positive and finite";
+    if (std::fabs(a[s] + b[s] - 1.) > 1e-14)
+      return "stage " + std::to_string(s) + ": a + b must be 1 (a consistent combination of states)";
+    // stage 0 reads the step's initial state: U0 + RHS(dt) when it is plainly
+    // that, else the general combination (both terms then read U0)
+    const bool first = s == 0 && c[s] == 1. && ((a[s] == 1. && b[s] == 0.) || (a[s] == 0. && b[s] == 1.));
+    sc.s[s] = swe::Stage{first, first ? 0. : a[s], first ? 0. : b[s], first ? 1. : c[s]};
+  }
+  *out = sc;
+  return "";
+}
+
 // Meshes from this many cells up choose their device order (SWE_REORDER_AUTO)
 // by timing each candidate; smaller ones by the gather cost model.
 constexpr int64_t kTimedLayoutCells = 1 << 16;
@@ -390,7 +412,7 @@ swe_status swe_set_stream(swe_ctx* ctx, void* stream) {
 swe_status swe_step(swe_ctx* ctx, int32_t scheme, double dt) {
   if (!ctx) return SWE_ERR_INVALID_ARGUMENT;
   SWE_GUARD_BEGIN
-  if (scheme < 0 || scheme > 2) return fail(&ctx->err, SWE_ERR_INVALID_ARGUMENT, "scheme must be 0, 1 or 2");
+  if (!ctx->eng.has_scheme(scheme)) return fail(&ctx->err, SWE_ERR_INVALID_ARGUMENT, kSchemeMsg);
   if (!(dt > 0.) || !std::isfinite(dt)) return fail(&ctx->err, SWE_ERR_INVALID_ARGUMENT, "dt must be positive and finite");
   cudaError_t e = cudaMemcpyAsync(ctx->eng.d_fixed_dt, &dt, sizeof(double), cudaMemcpyHostToDevice, ctx->eng.stream());
   // one replay of the step's CUDA graph (captured on first use)
@@ -403,7 +425,7 @@ swe_status swe_step(swe_ctx* ctx, int32_t scheme, double dt) {
 swe_status swe_run(swe_ctx* ctx, int32_t scheme, double dt, int64_t n_steps) {
   if (!ctx) return SWE_ERR_INVALID_ARGUMENT;
   SWE_GUARD_BEGIN
-  if (scheme < 0 || scheme > 2) return fail(&ctx->err, SWE_ERR_INVALID_ARGUMENT, "scheme must be 0, 1 or 2");
+  if (!ctx->eng.has_scheme(scheme)) return fail(&ctx->err, SWE_ERR_INVALID_ARGUMENT, kSchemeMsg);
   if (!(dt > 0.) || !std::isfinite(dt)) return fail(&ctx->err, SWE_ERR_INVALID_ARGUMENT, "dt must be positive and finite");
   if (n_steps < 0) return fail(&ctx->err, SWE_ERR_INVALID_ARGUMENT, "n_steps must be >= 0");
   cudaError_t e = cudaMemcpyAsync(ctx->eng.d_fixed_dt, &dt, sizeof(double), cudaMemcpyHostToDevice, ctx->eng.stream());
@@ -416,7 +438,7 @@ swe_status swe_run(swe_ctx* ctx, int32_t scheme, double dt, int64_t n_steps) {
 swe_status swe_run_cfl(swe_ctx* ctx, int32_t scheme, int64_t n_steps, double* t_elapsed) {
   if (!ctx) return SWE_ERR_INVALID_ARGUMENT;
   SWE_GUARD_BEGIN
-  if (scheme < 0 || scheme > 2) return fail(&ctx->err, SWE_ERR_INVALID_ARGUMENT, "scheme must be 0, 1 or 2");
+  if (!ctx->eng.has_scheme(scheme)) return fail(&ctx->err, SWE_ERR_INVALID_ARGUMENT, kSchemeMsg);
   if (n_steps < 0) return fail(&ctx->err, SWE_ERR_INVALID_ARGUMENT, "n_steps must be >= 0");
   cudaError_t e = ctx->eng.run_graph(scheme, 1, n_steps);
   if (e != cudaSuccess) return cuda_fail(&ctx->err, e, "swe_run_cfl");
@@ -593,13 +615,13 @@ swe_status swe_get_node_max(swe_ctx* ctx, double* max_out) {
 
 swe_status swe_time_kernels(swe_ctx* ctx, int32_t scheme, int64_t reps, double* out_ms) {
   if (!ctx || !out_ms) return SWE_ERR_INVALID_ARGUMENT;
-  if (scheme < 0 || scheme > 2 || reps <= 0) return fail(&ctx->err, SWE_ERR_INVALID_ARGUMENT, "bad scheme or reps");
+  if (!ctx->eng.has_scheme(scheme) || reps <= 0) return fail(&ctx->err, SWE_ERR_INVALID_ARGUMENT, "bad scheme or reps");
   double acc[6] = {0, 0, 0, 0, 0, 0};
   for (int64_t r = 0; r < reps; ++r) {
     cudaError_t e = ctx->eng.step_timed(scheme, 1, acc);
     if (e != cudaSuccess) return cuda_fail(&ctx->err, e, "swe_time_kernels");
   }
-  const int n_st = swe::scheme_table(scheme).n;
+  const int n_st = ctx->eng.scheme_of(scheme).n;
   for (int k = 0; k < 5; ++k) out_ms[k] = acc[k] / (double)(reps * n_st);
   out_ms[5] = acc[5] / (double)reps;
   return SWE_OK;
@@ -631,7 +653,7 @@ swe_status swe_adjoint_forward(swe_ctx* ctx, int32_t scheme, int64_t n_steps, in
                                int32_t n_gauges, const int64_t* gauge_cells, int64_t obs_every, double* traces_out) {
   if (!ctx) return SWE_ERR_INVALID_ARGUMENT;
   SWE_GUARD_BEGIN
-  if (scheme < 0 || scheme > 2 || n_steps <= 0 || checkpoint_every <= 0 || n_gauges < 0 || obs_every <= 0)
+  if (!ctx->eng.has_scheme(scheme) || n_steps <= 0 || checkpoint_every <= 0 || n_gauges < 0 || obs_every <= 0)
     return fail(&ctx->err, SWE_ERR_INVALID_ARGUMENT, "bad scheme, step counts or gauge count");
   if (n_gauges > 0 && (!gauge_cells || !traces_out))
     return fail(&ctx->err, SWE_ERR_INVALID_ARGUMENT, "gauge_cells and traces_out are required");
@@ -662,6 +684,17 @@ swe_status swe_adjoint_dts(swe_ctx* ctx, double* dts_out) {
   std::string e = ctx->eng.adjoint_dts(dts_out);
   if (!e.empty()) return fail(&ctx->err, SWE_ERR_INVALID_ARGUMENT, e);
   return SWE_OK;
+}
+
+swe_status swe_set_scheme(swe_ctx* ctx, int32_t n_stages, const double* a, const double* b, const double* c) {
+  if (!ctx) return SWE_ERR_INVALID_ARGUMENT;
+  SWE_GUARD_BEGIN
+  swe::Scheme sc;
+  std::string e = make_scheme(n_stages, a, b, c, &sc);
+  if (!e.empty()) return fail(&ctx->err, SWE_ERR_INVALID_ARGUMENT, e);
+  ctx->eng.set_custom_scheme(sc);
+  return SWE_OK;
+  SWE_GUARD_END(&ctx->err)
 }
 
 swe_status swe_get_tuning(swe_ctx* ctx, int32_t* out4) {
@@ -767,7 +800,7 @@ swe_status swe_batch_set_stream(swe_batch* b, void* stream) {
 
 swe_status swe_batch_run_cfl(swe_batch* b, int32_t scheme, int64_t n_steps) {
   if (!b) return SWE_ERR_INVALID_ARGUMENT;
-  if (scheme < 0 || scheme > 2 || n_steps < 0) return fail(&b->err, SWE_ERR_INVALID_ARGUMENT, "bad scheme or n_steps");
+  if (!b->eng.has_scheme(scheme) || n_steps < 0) return fail(&b->err, SWE_ERR_INVALID_ARGUMENT, "bad scheme or n_steps");
   cudaError_t e = b->eng.run_graph(scheme, 1, n_steps);
   if (e != cudaSuccess) return cuda_fail(&b->err, e, "swe_batch_run_cfl");
   return SWE_OK;
@@ -775,7 +808,7 @@ swe_status swe_batch_run_cfl(swe_batch* b, int32_t scheme, int64_t n_steps) {
 
 swe_status swe_batch_run(swe_batch* b, int32_t scheme, double dt, int64_t n_steps) {
   if (!b) return SWE_ERR_INVALID_ARGUMENT;
-  if (scheme < 0 || scheme > 2 || n_steps < 0) return fail(&b->err, SWE_ERR_INVALID_ARGUMENT, "bad scheme or n_steps");
+  if (!b->eng.has_scheme(scheme) || n_steps < 0) return fail(&b->err, SWE_ERR_INVALID_ARGUMENT, "bad scheme or n_steps");
   if (!(dt > 0.) || !std::isfinite(dt)) return fail(&b->err, SWE_ERR_INVALID_ARGUMENT, "dt must be positive and finite");
   const std::vector<double> dts((size_t)b->eng.I(), dt);  // the same dt for every instance
   cudaError_t e = cudaMemcpyAsync(b->eng.d_fixed_dt, dts.data(), dts.size() * sizeof(double), cudaMemcpyHostToDevice,
@@ -799,7 +832,7 @@ swe_status swe_batch_adjoint_forward(swe_batch* b, int32_t scheme, int64_t n_ste
                                      double* traces_out) {
   if (!b) return SWE_ERR_INVALID_ARGUMENT;
   SWE_GUARD_BEGIN
-  if (scheme < 0 || scheme > 2 || n_steps <= 0 || checkpoint_every <= 0 || n_gauges < 0 || obs_every <= 0)
+  if (!b->eng.has_scheme(scheme) || n_steps <= 0 || checkpoint_every <= 0 || n_gauges < 0 || obs_every <= 0)
     return fail(&b->err, SWE_ERR_INVALID_ARGUMENT, "bad scheme, step counts or gauge count");
   if (n_gauges > 0 && (!gauge_cells || !traces_out))
     return fail(&b->err, SWE_ERR_INVALID_ARGUMENT, "gauge_cells and traces_out are required");
@@ -841,6 +874,18 @@ swe_status swe_batch_integrals(swe_batch* b, int32_t q, double* out3) {
   if (e != cudaSuccess) return cuda_fail(&b->err, e, "swe_batch_integrals");
   return SWE_OK;
   SWE_GUARD_END(&b->err)
+}
+
+swe_status swe_batch_set_scheme(swe_batch* bt, int32_t n_stages, const double* a, const double* b,
+                                const double* c) {
+  if (!bt) return SWE_ERR_INVALID_ARGUMENT;
+  SWE_GUARD_BEGIN
+  swe::Scheme sc;
+  std::string e = make_scheme(n_stages, a, b, c, &sc);
+  if (!e.empty()) return fail(&bt->err, SWE_ERR_INVALID_ARGUMENT, e);
+  bt->eng.set_custom_scheme(sc);
+  return SWE_OK;
+  SWE_GUARD_END(&bt->err)
 }
 
 swe_status swe_batch_get_tuning(swe_batch* b, int32_t q, int32_t* out4) {

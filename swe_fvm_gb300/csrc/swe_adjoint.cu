@@ -866,6 +866,7 @@ struct AdjointState {
   std::vector<void*> allocs;
   // tape of the last taped forward run
   int scheme = 1;
+  Scheme sc{};  // the scheme's table at the taped run
   int64_t n_steps = 0, ckpt = 0, obs = 0;
   int n_gauges = 0;
   int* d_gauges = nullptr;
@@ -995,6 +996,7 @@ std::string Engine::adjoint_forward(int scheme, int64_t n_steps, int64_t ckpt, c
   a.free_tape();
   const int64_t C = mesh_.C;
   a.scheme = scheme;
+  a.sc = scheme_of(scheme);
   a.n_steps = n_steps;
   a.ckpt = ckpt;
   a.obs = obs;
@@ -1058,7 +1060,7 @@ std::string Engine::adjoint_backward(const double* trace_grads_host, double* gra
   AdjointState& a = *adj_;
   AdjWork& w = a.aw;
   const int64_t C = mesh_.C, N = mesh_.N;
-  const Scheme sc = scheme_table(a.scheme);
+  const Scheme sc = a.sc;
   const int ns = sc.n;
   const int64_t n_obs = a.obs > 0 ? a.n_steps / a.obs : 0;
   double* d_tg = nullptr;

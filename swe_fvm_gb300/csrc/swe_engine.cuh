@@ -113,10 +113,13 @@ struct Stage {
   double a, b, c; // U = a U0.cons + b Uprev.cons + RHS(c dt)
 };
 
+constexpr int kMaxStages = 4;
+constexpr int kCustomScheme = 3;  // id of the caller-defined table
 struct Scheme {
   int n;
-  Stage s[3];
+  Stage s[kMaxStages];
 };
+// Built-in schemes 0 Euler, 1 SSPRK2, 2 SSPRK3.
 Scheme scheme_table(int scheme);
 
 // Host-side description of one instance after validation.
@@ -151,6 +154,12 @@ class Engine {
   // Returns an empty string on success, else the error message (status in *st).
   // block > 0 fixes the threads per block of every cell and edge kernel.
   std::string init(std::vector<HostInstance>&& inst, int flux, int ws, int block, int* st, bool batched);
+
+  // Time schemes: 0..2 built in, kCustomScheme once set_custom_scheme defined
+  // it.  Changing the custom table drops its captured step graphs.
+  void set_custom_scheme(const Scheme& sc);
+  bool has_scheme(int id) const { return (id >= 0 && id <= 2) || (id == kCustomScheme && custom_.n > 0); }
+  Scheme scheme_of(int id) const { return id == kCustomScheme ? custom_ : scheme_table(id); }
 
   // Threads per block of the reconstruction kernels (k_recon1, k_recon2), the
   // edge-flux kernel (k_flux) and the drain/update kernels; drops the
@@ -280,7 +289,8 @@ class Engine {
   // copy of the state (3 x C) to or from buf; after a restore also zeroes the
   // accumulated time, the step dt and the error word
   cudaError_t snapshot(double* buf, bool restore);
-  cudaGraphExec_t graphs_[3][3] = {};
+  cudaGraphExec_t graphs_[4][3] = {};  // [scheme id][latch mode]
+  Scheme custom_{};
   AdjointState* adj_ = nullptr;
 };
 

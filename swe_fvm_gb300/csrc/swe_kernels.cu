@@ -868,10 +868,10 @@ void Engine::launch_update(const Stage& st, const double* const* in, const doubl
 }
 
 cudaError_t Engine::step_timed(int scheme, int latch_mode, double* acc) {
-  const Scheme sc = scheme_table(scheme);
+  const Scheme sc = scheme_of(scheme);
   double* S0[3] = {state(0, 0), state(0, 1), state(0, 2)};
   double* S1[3] = {state(1, 0), state(1, 1), state(1, 2)};
-  cudaEvent_t ev[3][6];
+  cudaEvent_t ev[kMaxStages][6];
   for (auto& row : ev)
     for (auto& x : row) cudaEventCreate(&x);
   cudaError_t e = cudaSuccess;
@@ -896,6 +896,15 @@ cudaError_t Engine::step_timed(int scheme, int latch_mode, double* acc) {
   for (auto& row : ev)
     for (auto& x : row) cudaEventDestroy(x);
   return e;
+}
+
+void Engine::set_custom_scheme(const Scheme& sc) {
+  custom_ = sc;
+  for (auto& g : graphs_[kCustomScheme])
+    if (g) {
+      cudaGraphExecDestroy(g);
+      g = nullptr;
+    }
 }
 
 void Engine::set_blocks(const int blocks[3]) {
@@ -1047,7 +1056,7 @@ cudaError_t Engine::stage_explicit(const Stage& st, const double* const* in, con
 }
 
 cudaError_t Engine::step(int scheme, int latch_mode) {
-  const Scheme sc = scheme_table(scheme);
+  const Scheme sc = scheme_of(scheme);
   double* S0[3] = {state(0, 0), state(0, 1), state(0, 2)};
   double* S1[3] = {state(1, 0), state(1, 1), state(1, 2)};
   for (int s = 0; s < sc.n; ++s) {
@@ -1092,7 +1101,7 @@ cudaError_t Engine::run_graph(int scheme, int latch_mode, int64_t n) {
     }
     launches_ = per_step;  // capture launched nothing
   }
-  const int64_t kernels_per_step = 6 * scheme_table(scheme).n;
+  const int64_t kernels_per_step = 6 * scheme_of(scheme).n;
   for (int64_t s = 0; s < n; ++s) {
     cudaError_t e = cudaGraphLaunch(ge, stream_);
     if (e != cudaSuccess) return e;

@@ -293,6 +293,11 @@ class SpaceDisc:
         self._check(_lib.load().swe_launch_count(self.ctx, ctypes.byref(n)))
         return n.value
 
+    def set_scheme(self, a, b, c) -> None:
+        """Defines scheme 3 (Solvers.Custom) as the Shu-Osher table (a, b, c)."""
+        a, b, c = _table(a, b, c)
+        self._check(_lib.load().swe_set_scheme(self.ctx, a.size, a.ctypes.data, b.ctypes.data, c.ctypes.data))
+
     def tuning(self) -> dict:
         """The device order and the threads per block the context runs with."""
         out = np.zeros(4, dtype=np.int32)
@@ -327,10 +332,33 @@ class TimeDisc:
         return dt.value
 
 
-class Solvers:
-    """Time schemes (include/Solvers.h:4-10): one step with a given dt."""
+def _table(a, b, c):
+    a, b, c = (np.ascontiguousarray(x, dtype=np.float64).reshape(-1) for x in (a, b, c))
+    if not (a.size == b.size == c.size):
+        raise ValueError("a, b and c need one entry per stage")
+    return a, b, c
 
-    EULER, SSPRK2_ID, SSPRK3_ID = 0, 1, 2
+
+def ssprk_m2(m: int):
+    """The m-stage, second-order strong-stability-preserving Runge-Kutta
+    scheme in Shu-Osher form (a, b, c): m - 1 forward-Euler stages of dt/(m-1),
+    then the average with the initial state; SSP coefficient m - 1."""
+    if m < 2:
+        raise ValueError("m >= 2")
+    a = [1.0] + [0.0] * (m - 2) + [1.0 / m]
+    b = [0.0] + [1.0] * (m - 2) + [(m - 1.0) / m]
+    c = [1.0 / (m - 1)] * (m - 1) + [1.0 / m]
+    return a, b, c
+
+
+class Solvers:
+    """Time schemes (include/Solvers.h:4-10): one step with a given dt.
+
+    A new scheme plugs in as a Shu-Osher table: ``sd.set_scheme(a, b, c)``
+    (stage s: a[s] U0 + b[s] U_{s-1} + RHS(U_{s-1}, c[s] dt)), then
+    ``Solvers.Custom(td, dt)`` or scheme id ``Solvers.CUSTOM`` in run/run_cfl."""
+
+    EULER, SSPRK2_ID, SSPRK3_ID, CUSTOM = 0, 1, 2, 3
 
     @staticmethod
     def _step(td: TimeDisc, scheme: int, dt: float):
@@ -349,8 +377,13 @@ class Solvers:
     def SSPRK3(td: TimeDisc, dt: float) -> None:
         Solvers._step(td, 2, dt)
 
+    @staticmethod
+    def Custom(td: TimeDisc, dt: float) -> None:
+        """One step of the table given to SpaceDisc.set_scheme."""
+        Solvers._step(td, 3, dt)
 
-SCHEMES = {"Euler": 0, "SSPRK2": 1, "SSPRK3": 2}
+
+SCHEMES = {"Euler": 0, "SSPRK2": 1, "SSPRK3": 2, "Custom": 3}
 
 
 class Batch:
@@ -424,6 +457,11 @@ class Batch:
         self._check(_lib.load().swe_batch_launch_count(self.b, ctypes.byref(n)))
         return n.value
 
+    def set_scheme(self, a, b, c) -> None:
+        """Defines scheme 3 for every instance as the Shu-Osher table (a, b, c)."""
+        a, b, c = _table(a, b, c)
+        self._check(_lib.load().swe_batch_set_scheme(self.b, a.size, a.ctypes.data, b.ctypes.data, c.ctypes.data))
+
     def tuning(self, q: int = 0) -> dict:
         """Device order of instance q and the batch's threads per block."""
         out = np.zeros(4, dtype=np.int32)
@@ -432,4 +470,4 @@ class Batch:
 
 
 __all__ = ["Topology", "Domain", "Wavespeeds", "Fluxes", "Fluxer", "SpaceDisc", "TimeDisc", "Solvers", "Batch",
-           "SweError", "SCHEMES", "REORDER", "layout_plan"]
+           "SweError", "SCHEMES", "REORDER", "layout_plan", "ssprk_m2"]
