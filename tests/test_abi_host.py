@@ -39,6 +39,18 @@ def test_header_compiles_as_c_and_cpp(tmp_path):
         assert r.returncode == 0, r.stderr
 
 
+def test_cpp_api_header_compiles():
+    """The reference-named C++ layer: Fluxes::HLLC<Wavespeeds::Einfeldt> names
+    a flux, SpaceDisc / TimeDisc / Solvers as in the reference."""
+    src = ('#include "swe_fvm_gb300.hpp"\n'
+           'static_assert(Fluxes::HLLC<Wavespeeds::Einfeldt>.flux == SWE_FLUX_HLLC, "");\n'
+           'static_assert(Fluxes::HLL<Wavespeeds::Davis>.wavespeed == SWE_WS_DAVIS, "");\n'
+           'void f(TimeDisc* td) { Solvers::SSPRK2(td, td->CFLdt()); }\n')
+    r = subprocess.run(["g++", "-std=c++17", "-Wall", "-Wextra", "-Werror", "-fsyntax-only", "-I",
+                        os.path.join(ROOT, "include"), "-x", "c++", "-"], input=src, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+
+
 def test_params_default_are_the_reference_values():
     L = _lib.load()
     p = _lib.SweParams()
