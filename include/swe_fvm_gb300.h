@@ -203,6 +203,17 @@ swe_status swe_synchronize(swe_ctx* ctx);
  * on this thread).  Never NULL. */
 const char* swe_last_error(swe_ctx* ctx);
 
+/* Simulated time accumulated by CFL runs (swe_run_cfl's t_elapsed); set it
+ * when resuming from a checkpoint.  No reference counterpart (its driver
+ * keeps t itself, examples/Main.cpp:237-241). */
+swe_status swe_get_time(swe_ctx* ctx, double* t);
+swe_status swe_set_time(swe_ctx* ctx, double t);
+/* Sets the CFL ratio that the next CFL step's dt is taken from (the
+ * reference's m_min_length_to_wavespeed, include/SpaceDisc.h:43): a resumed
+ * run takes the ratio its checkpoint recorded, which came from the last
+ * stage's flux pass, not from a pass over the final state. */
+swe_status swe_set_min_len_to_wavespeed(swe_ctx* ctx, double r);
+
 /* Time-scheme plugin: defines SWE_SCHEME_CUSTOM as a Shu-Osher table of
  * n_stages (1 to 4) stages, the form the reference's Solvers are written in
  * (src/Solvers.cpp:5-59): U_s = a[s] U0 + b[s] U_{s-1} + RHS(U_{s-1}, c[s] dt)
@@ -297,6 +308,12 @@ swe_status swe_batch_get_prim(swe_batch* b, int32_t instance, double* prim_out);
 /* Sum of the dts taken by an instance so far. */
 swe_status swe_batch_time(swe_batch* b, int32_t instance, double* t);
 swe_status swe_batch_launch_count(swe_batch* b, int64_t* n);
+/* Resume support for instance q of a batch: its time, its state (3 x C_q)
+ * and its CFL ratio. */
+swe_status swe_batch_set_time(swe_batch* b, int32_t q, double t);
+swe_status swe_batch_set_prim(swe_batch* b, int32_t q, const double* prim_in);
+swe_status swe_batch_min_len_to_wavespeed(swe_batch* b, int32_t q, double* r);
+swe_status swe_batch_set_min_len_to_wavespeed(swe_batch* b, int32_t q, double r);
 /* swe_set_scheme for every instance of a batch. */
 swe_status swe_batch_set_scheme(swe_batch* bt, int32_t n_stages, const double* a, const double* b, const double* c);
 /* swe_get_tuning for instance q of a batch (block sizes are shared). */

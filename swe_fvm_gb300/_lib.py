@@ -34,7 +34,9 @@ EXPORTS = [
     "swe_batch_get_prim", "swe_batch_time", "swe_batch_launch_count", "swe_batch_synchronize",
     "swe_batch_last_error", "swe_batch_adjoint_forward", "swe_batch_adjoint_backward", "swe_batch_adjoint_dts",
     "swe_integrals", "swe_batch_integrals", "swe_get_tuning", "swe_batch_get_tuning", "swe_layout_plan",
-    "swe_set_scheme", "swe_batch_set_scheme",
+    "swe_set_scheme", "swe_batch_set_scheme", "swe_get_time", "swe_set_time", "swe_batch_set_time",
+    "swe_batch_set_prim", "swe_set_min_len_to_wavespeed", "swe_batch_min_len_to_wavespeed",
+    "swe_batch_set_min_len_to_wavespeed",
 ]
 
 
@@ -72,19 +74,26 @@ class SweError(RuntimeError):
         super().__init__(f"{STATUS_NAMES.get(status, status)}: {message}")
 
 
+def checked() -> bool:
+    """SWE_GB300_CHECKED=1 selects the checked build (device range checks on
+    every gathered index of the step kernels) for this process."""
+    return os.environ.get("SWE_GB300_CHECKED", "0") == "1"
+
+
 def library_path() -> str:
-    return _build.LIB
+    return _build.LIB_CHECKED if checked() else _build.LIB
 
 
 def load(build_if_needed: bool = True):
     global _lib
     if _lib is not None:
         return _lib
+    path = library_path()
     if build_if_needed:
-        _build.build()
-    if not os.path.exists(_build.LIB):
-        raise RuntimeError(f"{_build.LIB} is missing: build it with swe_fvm_gb300.build.build()")
-    L = ctypes.CDLL(_build.LIB)
+        _build.build(checked=checked())
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is missing: build it with swe_fvm_gb300.build.build()")
+    L = ctypes.CDLL(path)
     vp, d, i32, i64 = ctypes.c_void_p, ctypes.c_double, ctypes.c_int32, ctypes.c_int64
     P = ctypes.POINTER
     sig = {
@@ -138,6 +147,13 @@ def load(build_if_needed: bool = True):
         "swe_layout_plan": [vp, i32, vp, vp, vp, vp, P(i32)],
         "swe_set_scheme": [vp, i32, vp, vp, vp],
         "swe_batch_set_scheme": [vp, i32, vp, vp, vp],
+        "swe_get_time": [vp, P(d)],
+        "swe_set_time": [vp, d],
+        "swe_batch_set_time": [vp, i32, d],
+        "swe_batch_set_prim": [vp, i32, vp],
+        "swe_set_min_len_to_wavespeed": [vp, d],
+        "swe_batch_min_len_to_wavespeed": [vp, i32, P(d)],
+        "swe_batch_set_min_len_to_wavespeed": [vp, i32, d],
     }
     for name, args in sig.items():
         f = getattr(L, name)

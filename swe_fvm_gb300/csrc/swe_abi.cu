@@ -14,6 +14,8 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "../../include/swe_fvm_gb300.h"
 #include "swe_engine.cuh"
 #include "swe_layout.cuh"
@@ -38,6 +40,16 @@ struct swe_batch {
 namespace {
 
 thread_local std::string g_create_error;
+
+// NVTX range over an entry point (host side: for graph replays it spans the
+// enqueue), named after the entry point, for timeline tools; free when no tool
+// is attached.
+struct Trace {
+  explicit Trace(const char* name) { nvtxRangePushA(name); }
+  ~Trace() { nvtxRangePop(); }
+  Trace(const Trace&) = delete;
+  Trace& operator=(const Trace&) = delete;
+};
 
 swe_status fail(std::string* slot, swe_status st, const std::string& msg) {
   if (slot) *slot = msg;
@@ -254,6 +266,8 @@ swe_status check_device(Engine& eng, std::string* err) {
   unsigned flags = 0;
   e = cudaMemcpy(&flags, eng.work().err, sizeof(unsigned), cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) return cuda_fail(err, e, "reading the device error word");
+  if (flags & swe::kErrBadIndex)
+    return fail(err, SWE_ERR_INVALID_MESH, "a kernel gathered an index out of range (checked build)");
   if (flags & swe::kErrNonFinite) return fail(err, SWE_ERR_NONFINITE, "a cell update produced a non-finite value");
   return SWE_OK;
 }
@@ -269,6 +283,7 @@ swe_status prime(Engine& eng, std::string* err) {
 }
 
 swe_status tune(Engine& eng, std::string* err) {
+  Trace trace("swe_tune_blocks");
   cudaError_t e = eng.autotune_blocks(1);
   if (e != cudaSuccess) return cuda_fail(err, e, "tuning the block sizes");
   return prime(eng, err);
@@ -307,6 +322,7 @@ swe_status build_ctx(HostInstance&& h, swe::Layout&& L, const swe_params& p, con
 // when the device has no room for it beside the best one.
 swe_status create_timed(const HostInstance& h, const swe_params& p, const double* prim0,
                         std::unique_ptr<swe_ctx>* out, std::string* why) {
+  Trace trace("swe_time_layouts");
   static const int kCand[3] = {SWE_REORDER_KEEP, SWE_REORDER_MORTON, SWE_REORDER_RCM};
   std::unique_ptr<swe_ctx> best;
   float best_ms = 0.f;
@@ -367,6 +383,7 @@ swe_status swe_params_default(swe_params* p) {
 }
 
 swe_status swe_create(const swe_mesh* mesh, const double* prim0, const swe_params* params, swe_ctx** out) {
+  Trace trace("swe_create");
   SWE_GUARD_BEGIN
   if (!out) return fail(nullptr, SWE_ERR_INVALID_ARGUMENT, "out is NULL");
   *out = nullptr;
@@ -410,6 +427,7 @@ swe_status swe_set_stream(swe_ctx* ctx, void* stream) {
 }
 
 swe_status swe_step(swe_ctx* ctx, int32_t scheme, double dt) {
+  Trace trace("swe_step");
   if (!ctx) return SWE_ERR_INVALID_ARGUMENT;
   SWE_GUARD_BEGIN
   if (!ctx->eng.has_scheme(scheme)) return fail(&ctx->err, SWE_ERR_INVALID_ARGUMENT, kSchemeMsg);
@@ -423,6 +441,7 @@ swe_status swe_step(swe_ctx* ctx, int32_t scheme, double dt) {
 }
 
 swe_status swe_run(swe_ctx* ctx, int32_t scheme, double dt, int64_t n_steps) {
+  Trace trace("swe_run");
   if (!ctx) return SWE_ERR_INVALID_ARGUMENT;
   SWE_GUARD_BEGIN
   if (!ctx->eng.has_scheme(scheme)) return fail(&ctx->err, SWE_ERR_INVALID_ARGUMENT, kSchemeMsg);
@@ -436,6 +455,7 @@ swe_status swe_run(swe_ctx* ctx, int32_t scheme, double dt, int64_t n_steps) {
 }
 
 swe_status swe_run_cfl(swe_ctx* ctx, int32_t scheme, int64_t n_steps, double* t_elapsed) {
+  Trace trace("swe_run_cfl");
   if (!ctx) return SWE_ERR_INVALID_ARGUMENT;
   SWE_GUARD_BEGIN
   if (!ctx->eng.has_scheme(scheme)) return fail(&ctx->err, SWE_ERR_INVALID_ARGUMENT, kSchemeMsg);
@@ -487,6 +507,7 @@ swe_status swe_compute_fluxes(swe_ctx* ctx) {
 }
 
 swe_status swe_integrals(swe_ctx* ctx, double* out3) {
+  Trace trace("swe_integrals");
   if (!ctx || !out3) return SWE_ERR_INVALID_ARGUMENT;
   SWE_GUARD_BEGIN
   cudaError_t e = ctx->eng.integrals(0, ctx->eng.C(), out3);
@@ -496,6 +517,7 @@ swe_status swe_integrals(swe_ctx* ctx, double* out3) {
 }
 
 swe_status swe_get_prim(swe_ctx* ctx, double* prim_out) {
+  Trace trace("swe_get_prim");
   if (!ctx || !prim_out) return SWE_ERR_INVALID_ARGUMENT;
   SWE_GUARD_BEGIN
   return download_prim(ctx->eng, prim_out, 0, ctx->eng.C(), &ctx->err);
@@ -503,6 +525,7 @@ swe_status swe_get_prim(swe_ctx* ctx, double* prim_out) {
 }
 
 swe_status swe_set_prim(swe_ctx* ctx, const double* prim_in) {
+  Trace trace("swe_set_prim");
   if (!ctx || !prim_in) return SWE_ERR_INVALID_ARGUMENT;
   SWE_GUARD_BEGIN
   // like assigning the reference's volume field: CFLdt() keeps the ratio of
@@ -651,6 +674,7 @@ const char* swe_last_error(swe_ctx* ctx) {
 
 swe_status swe_adjoint_forward(swe_ctx* ctx, int32_t scheme, int64_t n_steps, int64_t checkpoint_every,
                                int32_t n_gauges, const int64_t* gauge_cells, int64_t obs_every, double* traces_out) {
+  Trace trace("swe_adjoint_forward");
   if (!ctx) return SWE_ERR_INVALID_ARGUMENT;
   SWE_GUARD_BEGIN
   if (!ctx->eng.has_scheme(scheme) || n_steps <= 0 || checkpoint_every <= 0 || n_gauges < 0 || obs_every <= 0)
@@ -671,6 +695,7 @@ swe_status swe_adjoint_forward(swe_ctx* ctx, int32_t scheme, int64_t n_steps, in
 }
 
 swe_status swe_adjoint_backward(swe_ctx* ctx, const double* trace_grads, double* grad_prim0, double* grad_bathymetry) {
+  Trace trace("swe_adjoint_backward");
   if (!ctx || !grad_prim0 || !grad_bathymetry) return SWE_ERR_INVALID_ARGUMENT;
   SWE_GUARD_BEGIN
   std::string e = adjoint_backward_caller(ctx->eng, trace_grads, grad_prim0, grad_bathymetry);
@@ -695,6 +720,33 @@ swe_status swe_set_scheme(swe_ctx* ctx, int32_t n_stages, const double* a, const
   ctx->eng.set_custom_scheme(sc);
   return SWE_OK;
   SWE_GUARD_END(&ctx->err)
+}
+
+swe_status swe_get_time(swe_ctx* ctx, double* t) {
+  if (!ctx || !t) return SWE_ERR_INVALID_ARGUMENT;
+  cudaError_t e = cudaMemcpyAsync(t, ctx->eng.work().tsum, sizeof(double), cudaMemcpyDeviceToHost, ctx->eng.stream());
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->eng.stream());
+  if (e != cudaSuccess) return cuda_fail(&ctx->err, e, "swe_get_time");
+  return SWE_OK;
+}
+
+swe_status swe_set_time(swe_ctx* ctx, double t) {
+  if (!ctx) return SWE_ERR_INVALID_ARGUMENT;
+  if (!std::isfinite(t)) return fail(&ctx->err, SWE_ERR_INVALID_ARGUMENT, "t must be finite");
+  cudaError_t e = cudaMemcpyAsync(ctx->eng.work().tsum, &t, sizeof(double), cudaMemcpyHostToDevice, ctx->eng.stream());
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->eng.stream());
+  if (e != cudaSuccess) return cuda_fail(&ctx->err, e, "swe_set_time");
+  return SWE_OK;
+}
+
+swe_status swe_set_min_len_to_wavespeed(swe_ctx* ctx, double r) {
+  if (!ctx) return SWE_ERR_INVALID_ARGUMENT;
+  if (!(r > 0.) || !std::isfinite(r)) return fail(&ctx->err, SWE_ERR_INVALID_ARGUMENT, "r must be positive and finite");
+  const unsigned long long k = swe::order_key(r);
+  cudaError_t e = cudaMemcpyAsync(ctx->eng.work().r, &k, sizeof(k), cudaMemcpyHostToDevice, ctx->eng.stream());
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->eng.stream());
+  if (e != cudaSuccess) return cuda_fail(&ctx->err, e, "swe_set_min_len_to_wavespeed");
+  return SWE_OK;
 }
 
 swe_status swe_get_tuning(swe_ctx* ctx, int32_t* out4) {
@@ -742,6 +794,7 @@ swe_status swe_layout_plan(const swe_mesh* mesh, int32_t strategy, int64_t* cell
 // ------------------------------------------------------------------ batched
 swe_status swe_batch_create(int32_t n_instances, const swe_mesh* meshes, const double* const* prim0,
                             const swe_params* params, int32_t n_params, swe_batch** out) {
+  Trace trace("swe_batch_create");
   SWE_GUARD_BEGIN
   if (!out) return fail(nullptr, SWE_ERR_INVALID_ARGUMENT, "out is NULL");
   *out = nullptr;
@@ -799,6 +852,7 @@ swe_status swe_batch_set_stream(swe_batch* b, void* stream) {
 }
 
 swe_status swe_batch_run_cfl(swe_batch* b, int32_t scheme, int64_t n_steps) {
+  Trace trace("swe_batch_run_cfl");
   if (!b) return SWE_ERR_INVALID_ARGUMENT;
   if (!b->eng.has_scheme(scheme) || n_steps < 0) return fail(&b->err, SWE_ERR_INVALID_ARGUMENT, "bad scheme or n_steps");
   cudaError_t e = b->eng.run_graph(scheme, 1, n_steps);
@@ -807,6 +861,7 @@ swe_status swe_batch_run_cfl(swe_batch* b, int32_t scheme, int64_t n_steps) {
 }
 
 swe_status swe_batch_run(swe_batch* b, int32_t scheme, double dt, int64_t n_steps) {
+  Trace trace("swe_batch_run");
   if (!b) return SWE_ERR_INVALID_ARGUMENT;
   if (!b->eng.has_scheme(scheme) || n_steps < 0) return fail(&b->err, SWE_ERR_INVALID_ARGUMENT, "bad scheme or n_steps");
   if (!(dt > 0.) || !std::isfinite(dt)) return fail(&b->err, SWE_ERR_INVALID_ARGUMENT, "dt must be positive and finite");
@@ -830,6 +885,7 @@ swe_status swe_batch_get_prim(swe_batch* b, int32_t q, double* prim_out) {
 swe_status swe_batch_adjoint_forward(swe_batch* b, int32_t scheme, int64_t n_steps, int64_t checkpoint_every,
                                      int32_t n_gauges, const int64_t* gauge_cells, int64_t obs_every,
                                      double* traces_out) {
+  Trace trace("swe_batch_adjoint_forward");
   if (!b) return SWE_ERR_INVALID_ARGUMENT;
   SWE_GUARD_BEGIN
   if (!b->eng.has_scheme(scheme) || n_steps <= 0 || checkpoint_every <= 0 || n_gauges < 0 || obs_every <= 0)
@@ -851,6 +907,7 @@ swe_status swe_batch_adjoint_forward(swe_batch* b, int32_t scheme, int64_t n_ste
 
 swe_status swe_batch_adjoint_backward(swe_batch* b, const double* trace_grads, double* grad_prim0,
                                       double* grad_bathymetry) {
+  Trace trace("swe_batch_adjoint_backward");
   if (!b || !grad_prim0 || !grad_bathymetry) return SWE_ERR_INVALID_ARGUMENT;
   SWE_GUARD_BEGIN
   std::string e = adjoint_backward_caller(b->eng, trace_grads, grad_prim0, grad_bathymetry);
@@ -867,6 +924,7 @@ swe_status swe_batch_adjoint_dts(swe_batch* b, double* dts_out) {
 }
 
 swe_status swe_batch_integrals(swe_batch* b, int32_t q, double* out3) {
+  Trace trace("swe_batch_integrals");
   if (!b || !out3 || q < 0 || q >= b->eng.I()) return SWE_ERR_INVALID_ARGUMENT;
   SWE_GUARD_BEGIN
   const int64_t c0 = b->eng.cell_off[q], n = b->eng.cell_off[q + 1] - c0;
@@ -901,6 +959,44 @@ swe_status swe_batch_time(swe_batch* b, int32_t q, double* t) {
   if (e == cudaSuccess) e = cudaStreamSynchronize(b->eng.stream());
   if (e != cudaSuccess) return cuda_fail(&b->err, e, "swe_batch_time");
   return SWE_OK;
+}
+
+swe_status swe_batch_set_time(swe_batch* b, int32_t q, double t) {
+  if (!b || q < 0 || q >= b->eng.I()) return SWE_ERR_INVALID_ARGUMENT;
+  if (!std::isfinite(t)) return fail(&b->err, SWE_ERR_INVALID_ARGUMENT, "t must be finite");
+  cudaError_t e =
+      cudaMemcpyAsync(b->eng.work().tsum + q, &t, sizeof(double), cudaMemcpyHostToDevice, b->eng.stream());
+  if (e == cudaSuccess) e = cudaStreamSynchronize(b->eng.stream());
+  if (e != cudaSuccess) return cuda_fail(&b->err, e, "swe_batch_set_time");
+  return SWE_OK;
+}
+
+swe_status swe_batch_min_len_to_wavespeed(swe_batch* b, int32_t q, double* r) {
+  if (!b || !r || q < 0 || q >= b->eng.I()) return SWE_ERR_INVALID_ARGUMENT;
+  unsigned long long k = 0;
+  cudaError_t e = cudaMemcpyAsync(&k, b->eng.work().r + q, sizeof(k), cudaMemcpyDeviceToHost, b->eng.stream());
+  if (e == cudaSuccess) e = cudaStreamSynchronize(b->eng.stream());
+  if (e != cudaSuccess) return cuda_fail(&b->err, e, "swe_batch_min_len_to_wavespeed");
+  *r = swe::order_val(k);
+  return SWE_OK;
+}
+
+swe_status swe_batch_set_min_len_to_wavespeed(swe_batch* b, int32_t q, double r) {
+  if (!b || q < 0 || q >= b->eng.I()) return SWE_ERR_INVALID_ARGUMENT;
+  if (!(r > 0.) || !std::isfinite(r)) return fail(&b->err, SWE_ERR_INVALID_ARGUMENT, "r must be positive and finite");
+  const unsigned long long k = swe::order_key(r);
+  cudaError_t e = cudaMemcpyAsync(b->eng.work().r + q, &k, sizeof(k), cudaMemcpyHostToDevice, b->eng.stream());
+  if (e == cudaSuccess) e = cudaStreamSynchronize(b->eng.stream());
+  if (e != cudaSuccess) return cuda_fail(&b->err, e, "swe_batch_set_min_len_to_wavespeed");
+  return SWE_OK;
+}
+
+swe_status swe_batch_set_prim(swe_batch* b, int32_t q, const double* prim_in) {
+  if (!b || !prim_in || q < 0 || q >= b->eng.I()) return SWE_ERR_INVALID_ARGUMENT;
+  SWE_GUARD_BEGIN
+  const int64_t c0 = b->eng.cell_off[q], n = b->eng.cell_off[q + 1] - c0;
+  return upload_prim(b->eng, prim_in, c0, n, &b->err);
+  SWE_GUARD_END(&b->err)
 }
 
 swe_status swe_batch_launch_count(swe_batch* b, int64_t* n) {

@@ -24,7 +24,7 @@ constexpr int kComboStride = 12;  // doubles per full-wet combination record
 constexpr int kPw1Stride = 12;    // doubles per PartWet1 record
 constexpr int kDryStride = 8;     // doubles per dry-cell record
 
-enum : unsigned { kErrNonFinite = 1u, kErrBadState = 2u };
+enum : unsigned { kErrNonFinite = 1u, kErrBadState = 2u, kErrBadIndex = 4u };
 
 // PartWet2 (src/MUSCLObject.cpp:114-191) geometry: vertices sorted by z.
 struct Pw2Rec {
@@ -106,6 +106,23 @@ struct DevWork {
   const double* fixed_dt;      // [I] dt for fixed-step runs
   unsigned* err;               // [1] error bits
 };
+
+// A gathered index.  In checked builds (-DSWE_CHECKED, build(checked=True))
+// an index outside [0, n) sets kErrBadIndex and becomes 0, so the access stays
+// in bounds and the kernel's control flow (and its warp collectives) is
+// unchanged; the product build returns the index untouched.
+__device__ __forceinline__ int gidx(const DevWork& wk, int idx, int n) {
+#ifdef SWE_CHECKED
+  if ((unsigned)idx >= (unsigned)n) {
+    atomicOr(wk.err, kErrBadIndex);
+    return 0;
+  }
+#else
+  (void)wk;
+  (void)n;
+#endif
+  return idx;
+}
 
 // One Runge-Kutta stage in Shu-Osher form (src/Solvers.cpp:5-59).
 struct Stage {

@@ -152,7 +152,7 @@ __global__ void __launch_bounds__(256) k_recon1(DevMesh m, DevWork wk, const dou
       const double* dr = m.dry + (size_t)i * kDryStride;
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
-        node_max(wk, m.cnode[k * C + i], dr[k], m.zn[k * C + i]);
+        node_max(wk, gidx(wk, m.cnode[k * C + i], m.N), dr[k], m.zn[k * C + i]);
         const int slot = k * C + i;
         write_slot<COR0>(wk, slot, m.ze[slot], dr[3 + k], 0., 0., dr[6], dr[7], cor);
       }
@@ -166,7 +166,7 @@ __global__ void __launch_bounds__(256) k_recon1(DevMesh m, DevWork wk, const dou
         const double z = m.zn[k * C + i];
         double val;
         at_point_wet(wr, 0., z, &val);
-        node_max(wk, m.cnode[k * C + i], val, z);
+        node_max(wk, gidx(wk, m.cnode[k * C + i], m.N), val, z);
       }
       part = true;
       cls = 1;
@@ -177,7 +177,7 @@ __global__ void __launch_bounds__(256) k_recon1(DevMesh m, DevWork wk, const dou
       double wn[3];
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
-        const int nb = m.cnbr[k * C + i];  // never a wall: fully-wet cells are interior
+        const int nb = gidx(wk, m.cnbr[k * C + i], C);  // never a wall: fully-wet cells are interior
         const double wj = W[nb];
         wn[k] = wj;
         if (dlt(m.fwthr[nb], wj)) {
@@ -230,7 +230,7 @@ __global__ void __launch_bounds__(256) k_recon1(DevMesh m, DevWork wk, const dou
         const double zk = m.zn[slot];
         double val;
         at_point_wet(w, noff[k], zk, &val);
-        node_max(wk, m.cnode[slot], val, zk);
+        node_max(wk, gidx(wk, m.cnode[slot], m.N), val, zk);
         const double be = m.ze[slot];
         double we;
         if (at_point_wet(w, toff[k], be, &we)) write_slot<COR0>(wk, slot, be, we, u, v, gx, gy, cor);
@@ -258,7 +258,7 @@ __global__ void __launch_bounds__(256) k_recon2(DevMesh m, DevWork wk, const dou
   const int C = m.C;
   const int n = min(*wk.pwcount, C);
   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
-    const int i = wk.pwlist[q];
+    const int i = gidx(wk, wk.pwlist[q], C);
     const int inst = BATCH ? m.cinst[i] : 0;
     const double cor = m.inst_cor[inst];
     const double w = W[i], u = U[i], v = V[i];
@@ -268,7 +268,7 @@ __global__ void __launch_bounds__(256) k_recon2(DevMesh m, DevWork wk, const dou
     double gx = 0., gy = 0.;
     bool plane = false;
     if (!(dlt(b13, w) || r.flat)) {
-      const double w23 = order_val(wk.maxwp[r.lo]);
+      const double w23 = order_val(wk.maxwp[gidx(wk, r.lo, m.N)]);
       const double h23 = w23 - b23;
       const double ratio_b = r.ratio_b;
       const double h_delim1 = 1. / 3. * h23 * ratio_b;
@@ -331,7 +331,7 @@ __global__ void __launch_bounds__(256) k_recon2(DevMesh m, DevWork wk, const dou
 template <class FLUX, bool TAPE>
 __device__ __forceinline__ void flux_edge(const DevMesh& m, const DevWork& wk, const double* __restrict__ W, int e,
                                           int inst, double* lw) {
-  const int o = m.eown[e];
+  const int o = gidx(wk, m.eown[e], m.C);
   const int nb = m.enb[e];
   double F[3];
   const double nx = m.enx[e], ny = m.eny[e];
@@ -344,7 +344,7 @@ __device__ __forceinline__ void flux_edge(const DevMesh& m, const DevWork& wk, c
     g.tx = m.etx[e]; g.ty = m.ety[e];
     g.b = m.ezm[e];
     g.lmin = m.elmin[e];
-    const int sl = m.eslotl[e], sr = m.eslotr[e];
+    const int sl = gidx(wk, m.eslotl[e], 3 * m.C), sr = gidx(wk, m.eslotr[e], 3 * m.C);
     SideState L{wk.ew[sl], wk.eu[sl], wk.ev[sl]};
     SideState R{wk.ew[sr], wk.eu[sr], wk.ev[sr]};
     if (TAPE) FLUX::eval(g, L, R, m.inst_cor[inst], lw, F, EdgeTape{wk.ftape, m.E, e});
@@ -370,7 +370,7 @@ __global__ void __launch_bounds__(256) k_flux(DevMesh m, DevWork wk, const doubl
     bool mine = true;
     if (MODE == 1) {
       const int nb = m.enb[e];
-      mine = !(((wk.cls[m.eown[e]] & 3) == 1) || (nb >= 0 && (wk.cls[nb] & 3) == 1));
+      mine = !(((wk.cls[gidx(wk, m.eown[e], m.C)] & 3) == 1) || (nb >= 0 && (wk.cls[gidx(wk, nb, m.C)] & 3) == 1));
     }
     if (mine) flux_edge<FLUX, TAPE>(m, wk, W, e, inst, &lw);
   }
@@ -427,9 +427,9 @@ __global__ void __launch_bounds__(128) k_flux_pw(DevMesh m, DevWork wk, const do
   const int n = 3 * min(*wk.pwcount, C);
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
     const int q = t / 3, k = t - 3 * q;
-    const int i = wk.pwlist[q];
-    const int e = m.cedge[k * C + i];
-    const int o = m.eown[e];
+    const int i = gidx(wk, wk.pwlist[q], C);
+    const int e = gidx(wk, m.cedge[k * C + i], m.E);
+    const int o = gidx(wk, m.eown[e], C);
     if ((((wk.cls[o] & 3) == 1) ? o : m.enb[e]) != i) continue;
     const int inst = BATCH ? m.einst[e] : 0;
     double lw = kInf;
@@ -455,7 +455,7 @@ __global__ void __launch_bounds__(256) k_drain(DevMesh m, DevWork wk, const doub
     double sum = 0.;
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-      const double f = wk.f0[m.cedge[k * m.C + i]];
+      const double f = wk.f0[gidx(wk, m.cedge[k * m.C + i], m.E)];
       sum += smax(0., ((own >> k) & 1u) ? f : -f);
     }
     d = dgtc(sum, kTol) ? SWE_DIV(m.area[i] * h, sum) : kInf;
@@ -486,12 +486,12 @@ __global__ void __launch_bounds__(256) k_update(DevMesh m, DevWork wk, const dou
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
     const int slot = k * C + i;
-    const int e = m.cedge[slot];
+    const int e = gidx(wk, m.cedge[slot], m.E);
     // sgn = +1 for the edge's owner, else -1: products with it are sign changes
     const bool out = (own >> k) & 1u;
     const double F0 = wk.f0[e], F1 = wk.f1[e], F2 = wk.f2[e];
     const int nb = m.cnbr[slot];
-    const double dtik = nb < 0 ? kInf : wk.drain[nb];
+    const double dtik = nb < 0 ? kInf : wk.drain[gidx(wk, nb, C)];
     const double dtk = (out ? dgt0(F0) : dlt(F0, 0.)) ? smin(dt, dti) : smin(dt, dtik);  // sgn F0 > 0
     const double c_ek = m.cek[slot];
     const double h_ek = wk.ew[slot] - m.ze[slot];

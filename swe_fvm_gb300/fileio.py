@@ -8,14 +8,21 @@
   (examples/Main.cpp:65-73, dumpFields).
 - ``dump_domain`` / ``load_domain``: node geometry and topology text files
   (examples/Main.cpp:126-170, dumpGeometry2 / dumpTopology / dumpDomain).
+- ``save_state`` / ``load_state``: binary checkpoints (the primitive field,
+  bit for bit, the simulated time and a fingerprint of the mesh), to resume a
+  run; the reference has text dumps only.
 """
 from __future__ import annotations
+
+import hashlib
+from typing import NamedTuple
 
 import numpy as np
 
 from .mesh import Mesh, build_topology, load_reference_dump
 
-__all__ = ["read_gmsh", "dump_fields", "dump_domain", "load_domain"]
+__all__ = ["read_gmsh", "dump_fields", "dump_domain", "load_domain", "save_state", "load_state",
+           "mesh_fingerprint", "State"]
 
 
 def _sections(text: str) -> dict:
@@ -140,3 +147,39 @@ def dump_domain(mesh: Mesh, geometry_path: str, topology_path: str) -> None:
 def load_domain(geometry_path: str, topology_path: str) -> Mesh:
     """The inverse of dump_domain."""
     return load_reference_dump(geometry_path, topology_path)
+
+
+def mesh_fingerprint(mesh: Mesh) -> str:
+    """SHA-256 of the mesh's geometry and topology arrays (their bytes in the
+    reference's layouts)."""
+    h = hashlib.sha256()
+    m = mesh.contiguous()
+    for a in (m.geometry, m.edge_nodes, m.edge_cells, m.cell_nodes, m.cell_edges, m.cell_neighbours):
+        h.update(np.asarray(a).tobytes())
+    return h.hexdigest()
+
+
+class State(NamedTuple):
+    prim: np.ndarray   # (C, 3) primitive field
+    time: float        # simulated time
+    step: int          # steps taken
+    cfl_ratio: float   # the CFL ratio the next step's dt comes from (nan: not recorded)
+
+
+def save_state(path: str, mesh: Mesh, prim, t: float = 0.0, step: int = 0, cfl_ratio: float = float("nan")) -> None:
+    """A checkpoint: the (C, 3) primitive field, the simulated time, the step
+    count, the CFL ratio of the last flux pass and the mesh fingerprint
+    (``.npz``; values stored bit for bit)."""
+    prim = np.ascontiguousarray(prim, dtype=np.float64).reshape(mesh.num_cells, 3)
+    with open(path, "wb") as fh:
+        np.savez(fh, prim=prim, time=np.float64(t), step=np.int64(step), cfl_ratio=np.float64(cfl_ratio),
+                 fingerprint=np.array(mesh_fingerprint(mesh)))
+
+
+def load_state(path: str, mesh: Mesh = None) -> State:
+    """The checkpoint's State; with ``mesh`` given, refuses a checkpoint
+    written for another mesh."""
+    with np.load(path) as z:
+        if mesh is not None and str(z["fingerprint"]) != mesh_fingerprint(mesh):
+            raise ValueError(f"{path}: checkpoint belongs to another mesh")
+        return State(z["prim"].copy(), float(z["time"]), int(z["step"]), float(z["cfl_ratio"]))

@@ -293,6 +293,38 @@ class SpaceDisc:
         self._check(_lib.load().swe_launch_count(self.ctx, ctypes.byref(n)))
         return n.value
 
+    def time(self) -> float:
+        """Simulated time accumulated by CFL runs."""
+        t = ctypes.c_double()
+        self._check(_lib.load().swe_get_time(self.ctx, ctypes.byref(t)))
+        return t.value
+
+    def set_time(self, t: float) -> None:
+        self._check(_lib.load().swe_set_time(self.ctx, float(t)))
+
+    def save(self, path: str, step: int = 0) -> None:
+        """Checkpoint of the state, the time and the CFL ratio (fileio.save_state)."""
+        from .fileio import save_state
+
+        save_state(path, self.domain.mesh(), self.GetVolField(), self.time(), step, self.GetMinLenToWavespeed())
+
+    def restore(self, path: str) -> int:
+        """Resumes from a checkpoint of this mesh: state, time and CFL ratio
+        (so the continued run equals the uninterrupted one bit for bit);
+        returns its step count.  A checkpoint without a ratio takes the
+        restored state's own flux pass."""
+        from .fileio import load_state
+
+        st = load_state(path, self.domain.mesh())
+        self.SetVolField(st.prim)
+        self.set_time(st.time)
+        if np.isfinite(st.cfl_ratio):
+            self._check(_lib.load().swe_set_min_len_to_wavespeed(self.ctx, st.cfl_ratio))
+        else:
+            self.ComputeInterfaceValues()
+            self.ComputeFluxes()
+        return st.step
+
     def set_scheme(self, a, b, c) -> None:
         """Defines scheme 3 (Solvers.Custom) as the Shu-Osher table (a, b, c)."""
         a, b, c = _table(a, b, c)
@@ -456,6 +488,22 @@ class Batch:
         n = ctypes.c_int64()
         self._check(_lib.load().swe_batch_launch_count(self.b, ctypes.byref(n)))
         return n.value
+
+    def set_prim(self, q: int, prim) -> None:
+        a = np.ascontiguousarray(prim, dtype=np.float64).reshape(self.sizes[q], 3)
+        self._check(_lib.load().swe_batch_set_prim(self.b, int(q), a.ctypes.data))
+
+    def set_time(self, q: int, t: float) -> None:
+        self._check(_lib.load().swe_batch_set_time(self.b, int(q), float(t)))
+
+    def min_len_to_wavespeed(self, q: int) -> float:
+        """Instance q's CFL ratio (its next CFL dt is cfl times this)."""
+        r = ctypes.c_double()
+        self._check(_lib.load().swe_batch_min_len_to_wavespeed(self.b, int(q), ctypes.byref(r)))
+        return r.value
+
+    def set_min_len_to_wavespeed(self, q: int, r: float) -> None:
+        self._check(_lib.load().swe_batch_set_min_len_to_wavespeed(self.b, int(q), float(r)))
 
     def set_scheme(self, a, b, c) -> None:
         """Defines scheme 3 for every instance as the Shu-Osher table (a, b, c)."""

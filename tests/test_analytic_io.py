@@ -5,7 +5,7 @@ import math
 import numpy as np
 import pytest
 
-from swe_fvm_gb300 import analytic, diagnostics, fileio
+from swe_fvm_gb300 import analytic, diagnostics, fileio, scenarios
 from swe_fvm_gb300.mesh import build_topology, structured_square
 
 
@@ -168,3 +168,17 @@ def test_initial_state_and_l2_error_of_exact_averages():
     p[wet, 1] = avg[wet, 1] / avg[wet, 0]
     p[wet, 2] = avg[wet, 2] / avg[wet, 0]
     assert np.all(diagnostics.l2_errors(m, p, s, 0.0, n=8) < 1e-13)
+
+
+def test_checkpoint_round_trip_is_bitwise_and_mesh_bound(tmp_path):
+    from swe_fvm_gb300.fileio import load_state, save_state
+
+    m, prim = scenarios.random_front_case(10, 1)
+    prim = prim + np.random.default_rng(0).normal(0, 1e-9, prim.shape)
+    save_state(str(tmp_path / "ck.npz"), m, prim, t=0.123456789, step=42, cfl_ratio=0.0123)
+    p2, t, step, r = load_state(str(tmp_path / "ck.npz"), m)
+    assert np.array_equal(p2.view(np.uint64), prim.view(np.uint64))
+    assert (t, step, r) == (0.123456789, 42, 0.0123)
+    other, _ = scenarios.random_front_case(10, 2)
+    with pytest.raises(ValueError):
+        load_state(str(tmp_path / "ck.npz"), other)
