@@ -7,6 +7,7 @@ API, mesh and workload generators, and the PyTorch autograd layer.
 """
 from .mesh import Mesh, build_topology, structured_square, jittered_delaunay  # noqa: F401
 from .solver import (  # noqa: F401
+    REORDER,
     SCHEMES,
     Batch,
     Domain,
@@ -18,6 +19,8 @@ from .solver import (  # noqa: F401
     TimeDisc,
     Topology,
     Wavespeeds,
+    layout_plan,
+    ssprk_m2,
 )
 
 __version__ = "0.1.0"

@@ -81,11 +81,6 @@ __global__ void k_add3(int C, const double* a, const double* b, double* out) {
   }
 }
 
-__global__ void k_seed_gauges(double* lamw, const int* g, int n, const double* grad) {
-  const int q = blockIdx.x * blockDim.x + threadIdx.x;
-  if (q < n) atomicAdd(lamw + g[q], grad[q]);
-}
-
 // the gauge seeds of step n = *s0 + loc, when it ends an observation window
 __global__ void k_seed_gauges_seg(double* lamw, const int* g, int n_g, const double* tg, const long long* s0,
                                   long long loc, long long obs) {

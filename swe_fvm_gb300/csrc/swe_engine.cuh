@@ -249,9 +249,6 @@ class Engine {
   // state (3 x C interleaved) and the node bathymetry (N).
   std::string adjoint_backward(const double* trace_grads_host, double* grad_prim_host, double* grad_z_host);
   std::string adjoint_dts(double* out_host);
-  // Runs `in` -> `out` for one stage with the engine's current dt (no latch).
-  cudaError_t stage_explicit(const Stage& st, const double* const* in, const double* const* u0, double* const* out,
-                             int latch_mode);
 
   int C() const { return mesh_.C; }
   int E() const { return mesh_.E; }

@@ -1050,11 +1050,6 @@ cudaError_t Engine::update_only(const Stage& st, const double* const* in, const 
   return cudaGetLastError();
 }
 
-cudaError_t Engine::stage_explicit(const Stage& st, const double* const* in, const double* const* u0,
-                                   double* const* out, int latch_mode) {
-  return launch_stage(st, in, u0, out, true, latch_mode);
-}
-
 cudaError_t Engine::step(int scheme, int latch_mode) {
   const Scheme sc = scheme_of(scheme);
   double* S0[3] = {state(0, 0), state(0, 1), state(0, 2)};
