@@ -38,6 +38,12 @@ import numpy as np  # noqa: E402
 # connectivity): per stage read prim 24 + write prim 24 + 6 ids 24 + node xyz
 # 24 x N/C ~ 12 = 84 B; stage 2 re-reads the step's initial state, 24 B.
 BYTES_PER_CELL_STEP = 2 * 84 + 24
+# FP64 instructions issued per SSPRK2 cell-step by the step kernels (ncu
+# smsp__sass_thread_inst_executed_op_fp64_pred_on, per stage: k_flux 73.7 per
+# edge x 1.5 edges per cell + k_update 74 + k_recon1 23.9 + k_drain 7 per cell,
+# plus the few part-wet cells): the bound of the step on GB300, whose FP64 pipe
+# issues one instruction per lane and cycle (DFMA = 2 flops).
+FP64_INST_PER_CELL_STEP = 440
 LATTICE = int(os.environ.get("SWE_BENCH_LATTICE", "708"))
 CFL = 0.15
 
@@ -291,7 +297,11 @@ def run_gpu(args):
             "peak": hbm, "unit": "GB/s", "frac": achieved / hbm, "peak_source": src,
             "algorithmic_bytes_per_launch": BYTES_PER_CELL_STEP * C,
             "traffic": TRAFFIC_PER_STEP.get(LATTICE),
-            "kernel_ms_per_launch": per, "fp64_peak_tflops_measured": fp64.value}
+            "kernel_ms_per_launch": per, "fp64_peak_tflops_measured": fp64.value,
+            "fp64_issue": {"inst_per_cell_step": FP64_INST_PER_CELL_STEP,
+                           "achieved_tinst_per_s": FP64_INST_PER_CELL_STEP * C / (ms_step * 1e-3) / 1e12,
+                           "peak_tinst_per_s": fp64.value / 2,
+                           "frac": FP64_INST_PER_CELL_STEP * C / (ms_step * 1e-3) / 1e12 / (fp64.value / 2)}}
 
     out = {
         "metric": "cell-updates/s (plain FP64 SSPRK2 step, 1M-triangle unstructured mesh)",
