@@ -356,8 +356,11 @@ def run_layouts(torch, stream, mesh, prim, steps, warmup):
         e1.record(stream)
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1) / steps
+        kt = sd.time_kernels(1, 3)
         out[label] = {"ms_per_step": ms, "cell_updates_per_s": m.num_cells / (ms * 1e-3), "tuning": sd.tuning(),
-                      "create_s": round(t_create, 2)}
+                      "create_s": round(t_create, 2),
+                      "kernel_ms": dict(zip(["recon_pass1", "recon_pass2", "flux", "draining_dt", "update"],
+                                            [round(float(x), 4) for x in kt[:5]]))}
         del sd
     return out
 
