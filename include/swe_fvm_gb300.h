@@ -59,9 +59,11 @@ typedef enum swe_wavespeed { SWE_WS_RUSANOV = 0, SWE_WS_DAVIS = 1, SWE_WS_EINFEL
  * picks one of KEEP, MORTON, RCM: for meshes of 65,536 cells or more
  * swe_create builds a context in each order and keeps the one whose SSPRK2
  * steps run fastest (the caller's order unless another is more than 2 %
- * faster); smaller meshes and batch instances take the one with the fewest
- * 32-byte sectors gathered per warp (the caller's order unless another saves
- * more than 5 %). */
+ * faster), and so does swe_batch_create for batches of 65,536 cells or more
+ * whose instances all ask for AUTO (one order for every instance); smaller
+ * meshes and batches take, per instance, the one with the fewest 32-byte
+ * sectors gathered per warp (the caller's order unless another saves more
+ * than 5 %). */
 typedef enum swe_reorder {
   SWE_REORDER_AUTO = -1,
   SWE_REORDER_KEEP = 0,

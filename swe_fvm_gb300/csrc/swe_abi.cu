@@ -310,6 +310,10 @@ swe_status build_ctx(HostInstance&& h, swe::Layout&& L, const swe_params& p, con
   if (st == SWE_OK) st = prime(ctx->eng, why);
   if (st == SWE_OK && p.block == 0) st = tune(ctx->eng, why);
   if (st != SWE_OK) return st;
+  // creation returns with the priming pass done (the caller may move the
+  // context to another stream next)
+  cudaError_t e2 = cudaStreamSynchronize(ctx->eng.stream());
+  if (e2 != cudaSuccess) return cuda_fail(why, e2, "priming flux pass");
   *out = std::move(ctx);
   return SWE_OK;
 }
@@ -345,6 +349,81 @@ swe_status create_timed(const HostInstance& h, const swe_params& p, const double
     if (e == cudaSuccess) e = c->eng.time_steps(1, kTimedLayoutSteps, &ms2);
     if (e != cudaSuccess) return cuda_fail(why, e, "timing a device order");
     st = prime(c->eng, why);
+    if (st == SWE_OK && cudaStreamSynchronize(c->eng.stream()) != cudaSuccess)
+      st = cuda_fail(why, cudaGetLastError(), "priming flux pass");
+    if (st != SWE_OK) return st;
+    ms = std::min(ms, ms2);
+    if (!best || ms < 0.98f * best_ms) {
+      best = std::move(c);
+      best_ms = ms;
+    }
+  }
+  *out = std::move(best);
+  return SWE_OK;
+}
+
+// A batch over validated instances already in the device orders of lay.
+swe_status build_batch(std::vector<HostInstance>&& inst, std::vector<swe::Layout>&& lay, const swe_params& p0,
+                       const double* const* prim0, std::unique_ptr<swe_batch>* out, std::string* why) {
+  const int n = (int)inst.size();
+  std::unique_ptr<swe_batch> b(new swe_batch());
+  int ist = 0;
+  std::string e = b->eng.init(std::move(inst), p0.flux, p0.wavespeed, p0.block, &ist, true);
+  if (!e.empty()) return fail(why, (swe_status)ist, e);
+  e = b->eng.set_layouts(std::move(lay));
+  if (!e.empty()) return fail(why, SWE_ERR_CUDA, e);
+  for (int q = 0; q < n; ++q) {
+    const int64_t c0 = b->eng.cell_off[q], c = b->eng.cell_off[q + 1] - c0;
+    swe_status st = upload_prim(b->eng, prim0[q], c0, c, why);
+    if (st != SWE_OK) {
+      *why = "instance " + std::to_string(q) + ": " + *why;
+      return st;
+    }
+  }
+  swe_status st = prime(b->eng, why);
+  if (st == SWE_OK && p0.block == 0) st = tune(b->eng, why);
+  if (st != SWE_OK) return st;
+  cudaError_t e2 = cudaStreamSynchronize(b->eng.stream());
+  if (e2 != cudaSuccess) return cuda_fail(why, e2, "priming flux pass");
+  *out = std::move(b);
+  return SWE_OK;
+}
+
+// SWE_REORDER_AUTO for a batch of 65,536 cells or more: the same timed choice
+// as for a single context, over batches whose instances all take one order
+// (the callers', Morton, RCM).
+swe_status create_batch_timed(const std::vector<HostInstance>& inst, const swe_params& p0, const double* const* prim0,
+                              std::unique_ptr<swe_batch>* out, std::string* why) {
+  Trace trace("swe_time_layouts");
+  static const int kCand[3] = {SWE_REORDER_KEEP, SWE_REORDER_MORTON, SWE_REORDER_RCM};
+  const size_t n = inst.size();
+  std::unique_ptr<swe_batch> best;
+  float best_ms = 0.f;
+  for (int s : kCand) {
+    if (best) {
+      size_t free_b = 0, total_b = 0;
+      if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) break;
+      if (free_b < best->eng.device_bytes() + best->eng.device_bytes() / 4 + (size_t(256) << 20)) break;
+    }
+    std::vector<HostInstance> d(n);
+    std::vector<swe::Layout> L(n);
+    for (size_t q = 0; q < n; ++q) {
+      L[q] = swe::make_layout(inst[q], s);
+      d[q] = L[q].identity() ? inst[q] : swe::apply_layout(inst[q], L[q]);
+    }
+    std::unique_ptr<swe_batch> c;
+    swe_status st = build_batch(std::move(d), std::move(L), p0, prim0, &c, why);
+    if (st != SWE_OK) {
+      if (best) break;
+      return st;
+    }
+    float ms = 0.f, ms2 = 0.f;
+    cudaError_t e = c->eng.time_steps(1, kTimedLayoutSteps, &ms);
+    if (e == cudaSuccess) e = c->eng.time_steps(1, kTimedLayoutSteps, &ms2);
+    if (e != cudaSuccess) return cuda_fail(why, e, "timing a device order");
+    st = prime(c->eng, why);
+    if (st == SWE_OK && cudaStreamSynchronize(c->eng.stream()) != cudaSuccess)
+      st = cuda_fail(why, cudaGetLastError(), "priming flux pass");
     if (st != SWE_OK) return st;
     ms = std::min(ms, ms2);
     if (!best || ms < 0.98f * best_ms) {
@@ -802,11 +881,13 @@ swe_status swe_batch_create(int32_t n_instances, const swe_mesh* meshes, const d
   if (params && n_params != 1 && n_params != n_instances)
     return fail(nullptr, SWE_ERR_INVALID_ARGUMENT, "n_params must be 1 or n_instances");
   std::vector<HostInstance> inst(n_instances);
-  std::vector<swe::Layout> lay(n_instances);
+  std::vector<int> reorder(n_instances);
   swe_params p0;
   swe_params_default(&p0);
   if (params) p0 = params[0];
   std::string why;
+  bool all_auto = true;
+  int64_t total = 0;
   for (int q = 0; q < n_instances; ++q) {
     swe_params p = p0;
     if (params && n_params == n_instances) p = params[q];
@@ -816,22 +897,28 @@ swe_status swe_batch_create(int32_t n_instances, const swe_mesh* meshes, const d
       return fail(nullptr, SWE_ERR_UNSUPPORTED, "all instances of a batch must use the same flux and wave speed");
     if (!prim0[q]) return fail(nullptr, SWE_ERR_INVALID_ARGUMENT, "prim0[" + std::to_string(q) + "] is NULL");
     st = read_instance(&meshes[q], &p, &inst[q], &why);
-    if (st == SWE_OK) st = lay_out(&inst[q], p.reorder, &lay[q], &why);
+    if (st == SWE_OK) {
+      why = swe::validate_instance(inst[q]);
+      if (!why.empty()) st = SWE_ERR_INVALID_MESH;
+    }
     if (st != SWE_OK) return fail(nullptr, st, "instance " + std::to_string(q) + ": " + why);
+    reorder[q] = p.reorder;
+    all_auto = all_auto && p.reorder == SWE_REORDER_AUTO;
+    total += inst[q].C;
   }
-  std::unique_ptr<swe_batch> b(new swe_batch());
-  int ist = 0;
-  std::string e = b->eng.init(std::move(inst), p0.flux, p0.wavespeed, p0.block, &ist, true);
-  if (!e.empty()) return fail(nullptr, (swe_status)ist, e);
-  e = b->eng.set_layouts(std::move(lay));
-  if (!e.empty()) return fail(nullptr, SWE_ERR_CUDA, e);
-  for (int q = 0; q < n_instances; ++q) {
-    const int64_t c0 = b->eng.cell_off[q], n = b->eng.cell_off[q + 1] - c0;
-    swe_status st = upload_prim(b->eng, prim0[q], c0, n, &why);
-    if (st != SWE_OK) return fail(nullptr, st, "instance " + std::to_string(q) + ": " + why);
+  std::unique_ptr<swe_batch> b;
+  swe_status st;
+  if (all_auto && total >= kTimedLayoutCells) {
+    st = create_batch_timed(inst, p0, prim0, &b, &why);
+  } else {
+    std::vector<swe::Layout> lay(n_instances);
+    st = SWE_OK;
+    for (int q = 0; q < n_instances && st == SWE_OK; ++q) {
+      st = lay_out(&inst[q], reorder[q], &lay[q], &why);
+      if (st != SWE_OK) why = "instance " + std::to_string(q) + ": " + why;
+    }
+    if (st == SWE_OK) st = build_batch(std::move(inst), std::move(lay), p0, prim0, &b, &why);
   }
-  swe_status st = prime(b->eng, &why);
-  if (st == SWE_OK && p0.block == 0) st = tune(b->eng, &why);
   if (st != SWE_OK) return fail(nullptr, st, why);
   *out = b.release();
   return SWE_OK;

@@ -207,7 +207,10 @@ class Engine {
   size_t device_bytes() const { return bytes_; }
 
   // NULL selects the engine's own non-blocking stream.
-  void set_stream(cudaStream_t s) { stream_ = s ? s : own_stream_; }
+  // Work already enqueued on the previous stream is ordered before anything
+  // enqueued on the new one (an event recorded on the old stream, waited on
+  // by the new one).
+  void set_stream(cudaStream_t s);
   cudaStream_t stream() const { return stream_; }
 
   // Resets the node maxima and the part-wet list (done by k_drain at the end

@@ -566,7 +566,24 @@ T* Engine::dalloc(size_t n) {
   return (T*)p;
 }
 
+void Engine::set_stream(cudaStream_t s) {
+  cudaStream_t next = s ? s : own_stream_;
+  if (next == stream_) return;
+  cudaEvent_t ev = nullptr;
+  if (stream_ && cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) == cudaSuccess) {
+    if (cudaEventRecord(ev, stream_) == cudaSuccess) cudaStreamWaitEvent(next, ev, 0);
+    cudaEventDestroy(ev);  // released once the wait is satisfied
+  } else if (stream_) {
+    cudaStreamSynchronize(stream_);
+  }
+  stream_ = next;
+}
+
 Engine::~Engine() {
+  // nothing of this engine may still run on its own streams when its memory
+  // goes (a caller's stream is synchronised by swe_destroy)
+  if (own_stream_) cudaStreamSynchronize(own_stream_);
+  if (side_) cudaStreamSynchronize(side_);
   if (adj_) adjoint_state_delete(adj_);
   for (auto& row : graphs_)
     for (auto& g : row)
@@ -690,6 +707,7 @@ std::string Engine::init(std::vector<HostInstance>&& inst, int flux, int ws, int
   cudaMemset(Wk.f1, 0, E * sizeof(double));
   cudaMemset(Wk.f2, 0, E * sizeof(double));
   cudaMemset(Wk.pwcount, 0, sizeof(int));
+  cudaMemset(Wk.pwlist, 0, C * sizeof(int));  // every entry a valid cell id from the start
   cudaMemset(Wk.dt, 0, I * sizeof(double));
   cudaMemset(Wk.tsum, 0, I * sizeof(double));
   cudaMemset(Wk.err, 0, sizeof(unsigned));

@@ -169,3 +169,18 @@ def test_timed_order_choice_on_a_large_mesh(gpu):
     assert np.array_equal(a.GetVolField(), k.GetVolField())
     assert ta == tk
     assert np.array_equal(a.integrals(), k.integrals())
+
+
+def test_timed_order_choice_for_a_large_batch(gpu):
+    """A batch of 65,536 cells or more times one order for all instances; each
+    instance still equals its single context."""
+    cases = [scenarios.dam_break(120, seed_mesh=q) for q in range(3)]
+    assert sum(c[0].num_cells for c in cases) >= 1 << 16
+    b = Batch([c[0] for c in cases], [c[1] for c in cases], Fluxes.HLLC(Wavespeeds.Einfeldt), cfl=0.3)
+    orders = {b.tuning(q)["reorder"] for q in range(3)}
+    assert len(orders) == 1 and orders <= {"keep", "morton", "rcm"}
+    b.run_cfl(1, 8)
+    for q, (m, p) in enumerate(cases):
+        sd, t = _run(m, p, 8, reorder="keep")
+        assert np.array_equal(b.prim(q), sd.GetVolField()), q
+        assert b.time(q) == t
