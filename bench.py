@@ -398,6 +398,7 @@ def run_ensemble(torch, stream):
     ms_b = e0.elapsed_time(e1)
     launches_b = b.launch_count() - n0
     b.synchronize()
+    tuning_b = b.tuning(0)
     del b
     # plain, one instance after another
     sds = []
@@ -422,7 +423,8 @@ def run_ensemble(torch, stream):
             "plain_sequential_value": vp, "speedup_vs_plain": vb / vp, "instances": len(ens), "cells": cells,
             "steps": K, "ms_per_step": ms_b / K, "plain_ms_per_step": ms_p / K, "gpu_launches": launches_b,
             "config": {"workload": "ensemble_256", "cells_per_instance": "log-uniform 2k-200k", "cfl": 0.4,
-                       "flux": "HLLC+Einfeldt", "scheme": "SSPRK2", "mesh_gen_s": round(t_gen, 1)}}
+                       "flux": "HLLC+Einfeldt", "scheme": "SSPRK2", "mesh_gen_s": round(t_gen, 1),
+                       "tuning": tuning_b}}
 
 
 ADJ_CELLS = int(os.environ.get("SWE_BENCH_ADJ_CELLS", "250000"))
