@@ -1,0 +1,42 @@
+"""Streams: a context or batch moved to a caller's stream (PyTorch's here)
+right after creation, or between runs, orders its earlier work before the
+later work and gives the same state as on its own stream."""
+import numpy as np
+import pytest
+
+from swe_fvm_gb300 import Batch, Fluxes, SpaceDisc, Wavespeeds, scenarios
+
+pytestmark = pytest.mark.gpu
+
+
+def test_moving_to_a_caller_stream_keeps_the_results(gpu):
+    import torch
+
+    m, prim = scenarios.dam_break(200)  # 79k cells: the timed device-order choice runs at creation
+    ref = SpaceDisc(Fluxes.HLLC(Wavespeeds.Einfeldt), m, prim)
+    t_ref = ref.run_cfl(1, 10)
+    s1, s2 = torch.cuda.Stream(), torch.cuda.Stream()
+    sd = SpaceDisc(Fluxes.HLLC(Wavespeeds.Einfeldt), m, prim)
+    sd.set_stream(s1.cuda_stream)  # straight after creation
+    sd.run_cfl(1, 4)
+    sd.set_stream(s2.cuda_stream)  # between runs, with s1 work possibly in flight
+    sd.run_cfl(1, 3)
+    sd.set_stream(0)               # back to the context's own stream
+    t = sd.run_cfl(1, 3)
+    assert np.array_equal(sd.GetVolField(), ref.GetVolField())
+    assert t == t_ref
+
+
+def test_batch_on_a_caller_stream(gpu):
+    import torch
+
+    cases = [scenarios.random_front_case(20, q) for q in range(3)]
+    a = Batch([c[0] for c in cases], [c[1] for c in cases], Fluxes.HLLC(Wavespeeds.Einfeldt), cfl=0.3)
+    a.run_cfl(1, 8)
+    s = torch.cuda.Stream()
+    b = Batch([c[0] for c in cases], [c[1] for c in cases], Fluxes.HLLC(Wavespeeds.Einfeldt), cfl=0.3)
+    b.set_stream(s.cuda_stream)
+    b.run_cfl(1, 8)
+    s.synchronize()
+    for q in range(3):
+        assert np.array_equal(a.prim(q), b.prim(q))
