@@ -122,3 +122,20 @@ def test_rejects_null_arguments_and_bad_params():
     assert L.swe_step(None, 1, 1e-3) == 1
     assert L.swe_destroy(None) == 1
     assert L.swe_last_error(None) is not None
+
+
+def test_reference_module_name_imports():
+    """``import SWE_FVM`` as with the reference's pybind module: Topology.create
+    with its six arguments, copied (the reference's binding keeps references)."""
+    import SWE_FVM
+
+    m, _ = _small()
+    args = [m.edge_nodes.copy(), m.edge_cells.copy(), m.cell_nodes.copy(), m.cell_edges.copy(),
+            m.cell_neighbours.copy()]
+    t = SWE_FVM.Topology.create(m.num_nodes, *args)
+    for a in args:
+        a[:] = -7  # the caller's arrays may change or go away
+    assert t.num_elements() == m.num_cells and t.num_edges() == m.num_edges
+    assert t.IsEdgeBoundary(int(np.argmax(m.edge_cells[:, 1] < 0)))
+    for name in ("Domain", "SpaceDisc", "TimeDisc", "Solvers", "Fluxes", "Wavespeeds", "gauge_rollout"):
+        assert hasattr(SWE_FVM, name)
