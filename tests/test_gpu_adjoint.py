@@ -82,8 +82,9 @@ def test_gradient_initial_surface_matches_central_differences(gpu, adjoint_run):
             fd.append((loss_of(traces_fn(m, p1, dts, gauges), target) - loss_of(traces_fn(m, p2, dts, gauges), target)) / (2 * eps))
         assert fd[0] == fd[1]  # the CPU restatement differenced the same way
         errs.append(abs(gp[c, 0] - fd[0]) / max(abs(fd[0]), 1e-30))
-    assert np.median(errs) < 1e-5, errs
-    assert max(errs) < 1e-3, errs
+    # central differences at eps = 1e-7 of a bit-deterministic forward: 1e-6
+    # relative away from limiter, wet/dry and HLLC branch switches
+    assert max(errs) < 1e-6, errs
 
 
 def test_gradient_bathymetry_matches_central_differences(gpu, adjoint_run):
@@ -109,8 +110,9 @@ def test_gradient_bathymetry_matches_central_differences(gpu, adjoint_run):
             fd.append(loss_of(gpu_traces(mm, prim, dts, gauges), target))
         d = (fd[0] - fd[1]) / (2 * eps)
         errs.append(abs(gz[nd] - d) / max(abs(d), 1e-30))
-    assert np.median(errs) < 1e-5, errs
-    assert max(errs) < 1e-3, errs
+    # central differences at eps = 1e-7 of a bit-deterministic forward: 1e-6
+    # relative away from limiter, wet/dry and HLLC branch switches
+    assert max(errs) < 1e-6, errs
 
 
 def test_autograd_function_matches_c_abi(gpu, adjoint_run):

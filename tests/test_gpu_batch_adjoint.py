@@ -83,5 +83,12 @@ def test_batch_w0_gradient_finite_differences(gpu, runs):
                 vals.append(float(np.sum((np.array(tr) - targets[q]) ** 2)))
             fd = (vals[0] - vals[1]) / (2 * eps)
             errs.append(abs(gp[c, 0] - fd) / max(abs(fd), 1e-30))
-    assert np.median(errs) < 1e-5, errs
+    # central differences at eps = 1e-7 of a bit-deterministic forward agree to
+    # 1e-6 relative away from branch switches.  These instances have bumps
+    # that emerge through the surface; two of the tested cells (measured:
+    # 3.8e-5 and 2.9e-4) see partially-wet films in their domain of
+    # dependence, where the reverse of PartWet1 is regularised below the depth
+    # 1e-3 and branch switches lie within reach, so the bound on all cells is
+    # looser than on the median
+    assert np.median(errs) < 1e-6, errs
     assert max(errs) < 1e-3, errs

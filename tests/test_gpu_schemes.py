@@ -114,5 +114,6 @@ def test_custom_scheme_adjoint_matches_central_differences(gpu):
         p2 = prim.copy(); p2[c, 0] -= eps
         fd = (loss(p1) - loss(p2)) / (2 * eps)
         errs.append(abs(gp[c, 0] - fd) / max(abs(fd), 1e-30))
-    assert np.median(errs) < 1e-5, errs
-    assert max(errs) < 1e-3, errs
+    # central differences at eps = 1e-7 of a bit-deterministic forward: 1e-6
+    # relative away from limiter, wet/dry and HLLC branch switches
+    assert max(errs) < 1e-6, errs
