@@ -1270,6 +1270,10 @@ std::string Engine::adjoint_backward(const double* trace_grads_host, double* gra
   return err;
 }
 
+// Threads per block of the reverse kernels: 128 (and 64) measured 3 % faster
+// backward passes than 256 on a 250k-cell mesh (1.83 vs 1.89 s for 2000 steps).
+constexpr int kReverseBlock = 128;
+
 cudaError_t Engine::adjoint_stage_reverse(const Stage& st, const double* const* in, const double* const* u0,
                                           AdjWork& aw) {
   // recompute the stage's forward intermediates from its input into work_
@@ -1277,7 +1281,7 @@ cudaError_t Engine::adjoint_stage_reverse(const Stage& st, const double* const* 
   if (e == cudaSuccess) e = interface_values(in[0], in[1], in[2], 0);
   if (e == cudaSuccess) e = fluxes(in[0]);
   if (e != cudaSuccess) return e;
-  const int b = 256;
+  const int b = kReverseBlock;
   k_drain_keep<<<(mesh_.C + b - 1) / b, b, 0, stream_>>>(mesh_, work_, in[0]);
   ++launches_;
   return adjoint_stage_reverse_stored(st, in, u0, aw, work_, nullptr);
@@ -1285,7 +1289,7 @@ cudaError_t Engine::adjoint_stage_reverse(const Stage& st, const double* const* 
 
 cudaError_t Engine::adjoint_stage_reverse_stored(const Stage& st, const double* const* in, const double* const* u0,
                                                  AdjWork& aw, const DevWork& wk, const double* nst) {
-  const int b = 256;
+  const int b = kReverseBlock;
   const int gc = (mesh_.C + b - 1) / b, ge = (mesh_.E + b - 1) / b;
   // the partially-wet cells' Jacobians need no adjoint: a side stream
   // computes them while R1-R3 run
