@@ -40,3 +40,36 @@ def test_batch_on_a_caller_stream(gpu):
     s.synchronize()
     for q in range(3):
         assert np.array_equal(a.prim(q), b.prim(q))
+
+
+def test_distinct_contexts_run_concurrently_from_host_threads(gpu):
+    """One context per host thread (each on its own stream): creation, tuning,
+    graph capture and runs proceed side by side and give the sequential
+    results."""
+    import threading
+
+    cases = [scenarios.random_front_case(24, q) for q in range(4)] + [scenarios.dam_break(190)]
+    want = []
+    for m, p in cases:
+        sd = SpaceDisc(Fluxes.HLLC(Wavespeeds.Einfeldt), m, p, cfl=0.3)
+        want.append((sd.run_cfl(1, 12), sd.GetVolField()))
+    got = [None] * len(cases)
+    errors = []
+
+    def work(q):
+        try:
+            m, p = cases[q]
+            sd = SpaceDisc(Fluxes.HLLC(Wavespeeds.Einfeldt), m, p, cfl=0.3)
+            got[q] = (sd.run_cfl(1, 12), sd.GetVolField())
+        except Exception as ex:  # reported below
+            errors.append(repr(ex))
+
+    threads = [threading.Thread(target=work, args=(q,)) for q in range(len(cases))]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join(timeout=600)
+    assert not errors, errors
+    for q in range(len(cases)):
+        assert got[q][0] == want[q][0]
+        assert np.array_equal(got[q][1], want[q][1]), q
