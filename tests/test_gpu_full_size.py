@@ -91,3 +91,37 @@ def test_ensemble_256_members_equal_single_contexts(gpu):
         t = sd.run_cfl(1, 6)
         assert np.array_equal(b.prim(q), sd.GetVolField()), q
         assert b.time(q) == t, q
+
+
+def test_adjoint_250k_linearity_and_tape(gpu):
+    """The adjoint configuration's mesh (250k cells): the taped forward equals
+    the plain steps bit for bit, and the backward pass is linear in the trace
+    gradients (doubling is exact up to the order of the atomic node sums,
+    superposition holds to round-off)."""
+    from swe_fvm_gb300.adjoint import Rollout
+
+    m, prim = scenarios.hump_instance(2024, 250_000)
+    m = m.contiguous()
+    gauges = np.random.default_rng(11).choice(m.num_cells, 64, replace=False)
+    n, obs = 100, 10
+    ro = Rollout(m, prim)
+    tr = ro.forward(1, n, 50, gauges, obs)
+    sd = SpaceDisc(Fluxes.HLLC(Wavespeeds.Einfeldt), m, prim)
+    td = TimeDisc(sd)
+    plain = []
+    for k, dt in enumerate(ro.dts(n)):
+        Solvers.SSPRK2(td, dt)
+        if (k + 1) % obs == 0:
+            plain.append(sd.GetVolField()[gauges, 0])
+    assert np.array_equal(tr, np.array(plain))
+    rng = np.random.default_rng(3)
+    g1, g2 = rng.normal(size=tr.shape), rng.normal(size=tr.shape)
+    p1, z1 = ro.backward(g1)
+    p2, z2 = ro.backward(g2)
+    p12, z12 = ro.backward(g1 + g2)
+    pd, zd = ro.backward(2.0 * g1)
+    for a, b in ((p1, pd), (z1, zd)):
+        assert np.all(np.isfinite(a)) and np.max(np.abs(a)) > 0
+        assert np.max(np.abs(2.0 * a - b)) <= 1e-13 * np.max(np.abs(b))
+    for a, b, c in ((p1, p2, p12), (z1, z2, z12)):
+        assert np.max(np.abs(a + b - c)) <= 1e-11 * np.max(np.abs(c))
