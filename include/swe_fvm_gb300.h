@@ -120,7 +120,10 @@ swe_status swe_create(const swe_mesh* mesh, const double* prim0, const swe_param
 swe_status swe_destroy(swe_ctx* ctx);
 
 /* Runs kernels of this context on `stream` (a cudaStream_t; NULL = the
- * context's own stream). */
+ * context's own stream).  Work already enqueued on the previous stream is
+ * ordered before anything enqueued on the new one; swe_create returns with
+ * its own device work finished.  The caller keeps `stream` alive while the
+ * context uses it. */
 swe_status swe_set_stream(swe_ctx* ctx, void* stream);
 
 /* One time step of the scheme with a fixed dt: Solvers::X(&td, dt)
@@ -299,7 +302,8 @@ swe_status swe_adjoint_dts(swe_ctx* ctx, double* dts_out);
 swe_status swe_batch_create(int32_t n_instances, const swe_mesh* meshes, const double* const* prim0,
                             const swe_params* params, int32_t n_params, swe_batch** out);
 swe_status swe_batch_destroy(swe_batch* b);
-/* Runs the batch's kernels on `stream` (NULL = the batch's own stream). */
+/* Runs the batch's kernels on `stream` (NULL = the batch's own stream), with
+ * the ordering of swe_set_stream. */
 swe_status swe_batch_set_stream(swe_batch* b, void* stream);
 /* n_steps steps of every instance, each with its own dt = cfl * ratio taken
  * before every step; one CUDA graph per step replayed n_steps times. */
