@@ -180,6 +180,23 @@ def run_gpu(args):
 
     dist, rank, world, local = dist_setup(args.gpus)
     torch.cuda.set_device(local)
+    if args.ensemble_profile:
+        # profiling driver for the batched form: the 256-instance ensemble,
+        # warm-up, then exactly K graph-replayed steps inside the profiled range
+        from swe_fvm_gb300 import Batch, Fluxes, Wavespeeds, scenarios
+
+        ens = scenarios.ensemble(ENSEMBLE_INSTANCES)
+        b = Batch([e[0] for e in ens], [e[1] for e in ens], Fluxes.HLLC(Wavespeeds.Einfeldt), cfl=0.4)
+        b.run_cfl(1, args.warmup)
+        b.synchronize()
+        torch.cuda.cudart().cudaProfilerStart()
+        b.run_cfl(1, args.steps)
+        b.synchronize()
+        torch.cuda.cudart().cudaProfilerStop()
+        print(json.dumps({"ensemble_profile": True, "instances": len(ens),
+                          "cells": int(sum(e[0].num_cells for e in ens)), "steps": args.steps,
+                          "tuning": b.tuning(0)}))
+        return
     mesh, prim, t_gen = workload()
     C = mesh.num_cells
     sd = SpaceDisc(Fluxes.HLLC(Wavespeeds.Einfeldt), mesh, prim, cfl=CFL)
@@ -619,6 +636,8 @@ def main():
     ap.add_argument("--adjoint-profile", action="store_true", help="only a short taped run and its reverse")
     ap.add_argument("--no-batch-adjoint", action="store_true", help="skip the batched-adjoint leg")
     ap.add_argument("--layouts", action="store_true", help="also time every device order of the mesh")
+    ap.add_argument("--ensemble-profile", action="store_true",
+                    help="only the batched ensemble: warm-up + K steps (for ncu captures)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
