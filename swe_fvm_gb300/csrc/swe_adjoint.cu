@@ -50,7 +50,7 @@ __global__ void __launch_bounds__(256) k_drain_keep(DevMesh m, DevWork wk, const
     double sum = 0.;
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-      const double f = wk.f0[m.cedge[k * m.C + i]];
+      const double f = wk.f0[gidx(m, m.cedge[k * m.C + i], m.E)];
       sum += smax(0., ((own >> k) & 1u) ? f : -f);
     }
     d = dgtc(sum, kTol) ? SWE_DIV(m.area[i] * h, sum) : kInfA;
@@ -121,9 +121,9 @@ __global__ void __launch_bounds__(256) k_adj_update(DevMesh m, DevWork wk, AdjWo
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
     const int slot = k * C + i;
-    const double F0 = wk.f0[m.cedge[slot]];
+    const double F0 = wk.f0[gidx(m, m.cedge[slot], m.E)];
     const int nb = m.cnbr[slot];
-    const double dtik = nb < 0 ? kInfA : wk.drain[nb];
+    const double dtik = nb < 0 ? kInfA : wk.drain[gidx(m, nb, C)];
     dtk_[k] = dgt0(((own >> k) & 1u) ? F0 : -F0) ? smin(dt, dti) : smin(dt, dtik);
   }
   const double h0 = W0[i] - b;
@@ -214,7 +214,7 @@ __global__ void __launch_bounds__(256) k_adj_update(DevMesh m, DevWork wk, AdjWo
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
     const int slot = k * C + i;
-    const int e = m.cedge[slot];
+    const int e = gidx(m, m.cedge[slot], m.E);
     const bool out = (own >> k) & 1u;
     const double F0 = wk.f0[e], F1 = wk.f1[e], F2 = wk.f2[e];
     const double c_ek = m.cek[slot];
@@ -243,7 +243,7 @@ __global__ void __launch_bounds__(256) k_adj_update(DevMesh m, DevWork wk, AdjWo
     if (dgt0(out ? F0 : -F0)) {
       if (dlt(dti, dt)) route = 1;
     } else if (nb >= 0) {
-      if (dlt(wk.drain[nb], dt)) route = 2;
+      if (dlt(wk.drain[gidx(m, nb, C)], dt)) route = 2;
     }
     aw.ldtk[slot] = route ? ldtk : 0.;
     aw.route[slot] = (unsigned char)route;
@@ -262,7 +262,10 @@ __global__ void __launch_bounds__(256) k_adj_drain(DevMesh m, DevWork wk, AdjWor
     const int slot = k * C + i;
     if (aw.route[slot] == 1) ld += aw.ldtk[slot];
     const int tw = aw.twin[slot];
-    if (tw >= 0 && aw.route[tw] == 2) ld += aw.ldtk[tw];
+    if (tw >= 0) {
+      const int t2 = gidx(m, tw, 3 * C);
+      if (aw.route[t2] == 2) ld += aw.ldtk[t2];
+    }
   }
   const double h = Wp[i] - m.bc[i];
 #pragma unroll
@@ -273,7 +276,7 @@ __global__ void __launch_bounds__(256) k_adj_drain(DevMesh m, DevWork wk, AdjWor
   double fk[3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
-    const double f = wk.f0[m.cedge[k * C + i]];
+    const double f = wk.f0[gidx(m, m.cedge[k * C + i], m.E)];
     fk[k] = ((own >> k) & 1u) ? f : -f;
     sum += smax(0., fk[k]);
   }
@@ -296,8 +299,8 @@ template <int FLUX, int WS>
 __global__ void __launch_bounds__(256) k_adj_flux(DevMesh m, DevWork wk, AdjWork aw, const double* Wp) {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= m.E) return;
-  const int o = m.eown[e], nb = m.enb[e];
-  const int sl = m.eslotl[e];
+  const int o = gidx(m, m.eown[e], m.C), nb = m.enb[e];
+  const int sl = gidx(m, m.eslotl[e], 3 * m.C);
   double lF[3] = {aw.lF0[sl] + aw.lF0d[sl], aw.lF1[sl], aw.lF2[sl]};
   const double nx = m.enx[e], ny = m.eny[e];
   if (nb < 0) {
@@ -307,7 +310,7 @@ __global__ void __launch_bounds__(256) k_adj_flux(DevMesh m, DevWork wk, AdjWork
     return;
   }
   aw.lhwall[sl] = 0.;
-  const int sr = m.eslotr[e];
+  const int sr = gidx(m, m.eslotr[e], 3 * m.C);
   lF[0] += aw.lF0[sr] + aw.lF0d[sr];
   lF[1] += aw.lF1[sr];
   lF[2] += aw.lF2[sr];
@@ -365,15 +368,15 @@ __device__ double pass1_node_value(const DevMesh& m, const DevWork& wk, const do
 }
 
 // node id of local node k of cell c
-__device__ __forceinline__ int cnode(const DevMesh& m, int c, int k) { return m.cnode[k * m.C + c]; }
+__device__ __forceinline__ int cnode(const DevMesh& m, int c, int k) { return gidx(m, m.cnode[k * m.C + c], m.N); }
 
 // adds l to the node-z gradient through the edge-centre bathymetry of slot
 // (c, k): the midpoint of the edge's two nodes
 __device__ __forceinline__ void lam_edge_z(const DevMesh& m, AdjWork& aw, int c, int k, double l) {
   if (l == 0.) return;
-  const int e = m.cedge[k * m.C + c];
-  atomicAdd(aw.lz + aw.edge_nodes[2 * e], 0.5 * l);
-  atomicAdd(aw.lz + aw.edge_nodes[2 * e + 1], 0.5 * l);
+  const int e = gidx(m, m.cedge[k * m.C + c], m.E);
+  atomicAdd(aw.lz + gidx(m, aw.edge_nodes[2 * e], m.N), 0.5 * l);
+  atomicAdd(aw.lz + gidx(m, aw.edge_nodes[2 * e + 1], m.N), 0.5 * l);
 }
 // ... through the centroid bathymetry of cell c
 __device__ __forceinline__ void lam_cell_z(const DevMesh& m, AdjWork& aw, int c, double l) {
@@ -530,12 +533,11 @@ __device__ void combo_plane_points(const DevMesh& m, int c, int mask, double* px
   const int C = m.C;
   const Pw2Rec& r = m.pw2[c];
   for (int k = 0; k < 3; ++k) {
-    const int nb = m.cnbr[k * C + c];
     if ((mask >> k) & 1) {
       px[k] = r.dedge[k][0];
       py[k] = r.dedge[k][1];
     } else {
-      const Pw2Rec& rn = m.pw2[nb];
+      const Pw2Rec& rn = m.pw2[gidx(m, m.cnbr[k * C + c], C)];
       px[k] = (rn.p[0][0] + rn.tp0x) - (r.p[0][0] + r.tp0x);
       py[k] = (rn.p[0][1] + rn.tp0y) - (r.p[0][1] + r.tp0y);
     }
@@ -546,7 +548,7 @@ __device__ void combo_points_to_nodes(const DevMesh& m, AdjWork& aw, int c, int 
   for (int k = 0; k < 3; ++k) {
     if (lp[k] == 0.) continue;
     if ((mask >> k) & 1) lam_edge_z(m, aw, c, k, lp[k]);
-    else lam_cell_z(m, aw, m.cnbr[k * m.C + c], lp[k]);
+    else lam_cell_z(m, aw, gidx(m, m.cnbr[k * m.C + c], m.C), lp[k]);
   }
 }
 
@@ -580,7 +582,7 @@ __device__ void pw_jacobian(const DevMesh& m, const DevWork& wk, const AdjWork& 
   const int C = m.C;
   const double w = W[i];
   const Pw2Rec& r = m.pw2[i];
-  const double w23 = order_val(wk.maxwp[r.lo]);
+  const double w23 = order_val(wk.maxwp[gidx(m, r.lo, m.N)]);
   typedef Dual<5> D5;  // PartWet2 over (w, w23, z_lo, z_mid, z_hi)
   D5 zc[3];
   for (int k = 0; k < 3; ++k) zc[k] = D5(m.zn[k * C + i]);
@@ -621,10 +623,11 @@ __device__ void pw_jacobian(const DevMesh& m, const DevWork& wk, const AdjWork& 
     J.jgy[q] = gyD.d[q];
   }
   // w23 = max over the cells around the lowest node of their pass-1 value
-  const int nd = r.lo;
+  const int nd = gidx(m, r.lo, m.N);
   int best = -1, bestk = 0;
   for (int q = aw.node_ptr[nd]; q < aw.node_ptr[nd + 1]; ++q) {
-    const int c = aw.node_cells[q] >> 2, kn = aw.node_cells[q] & 3;
+    const int cq = aw.node_cells[gidx(m, q, 3 * C)];
+    const int c = gidx(m, cq >> 2, C), kn = cq & 3;
     if (pass1_node_value(m, wk, W, c, kn) == w23) {
       best = c;
       bestk = kn;
@@ -811,21 +814,21 @@ __device__ void adj_recon_cell(const DevMesh& m, const DevWork& wk, AdjWork aw, 
     if (g1 != 0.) {
       const int t = J->target;
       switch (J->route) {
-        case 0: atomicAdd(aw.lz + t, g1); break;
+        case 0: atomicAdd(aw.lz + gidx(m, t, m.N), g1); break;
         case 1:
-          for (int q = 0; q < 3; ++q) atomicAdd(aw.lz + cnode(m, t, q), g1 * J->rc[q]);
+          for (int q = 0; q < 3; ++q) atomicAdd(aw.lz + cnode(m, gidx(m, t, C), q), g1 * J->rc[q]);
           break;
         case 2:
-          atomicAdd(aw.lscatter + t, g1);
+          atomicAdd(aw.lscatter + gidx(m, t, C), g1);
           if (J->mask >= 0) {
             const double lp[3] = {g1 * J->rc[0], g1 * J->rc[1], g1 * J->rc[2]};
-            combo_points_to_nodes(m, aw, t, J->mask, lp);
+            combo_points_to_nodes(m, aw, gidx(m, t, C), J->mask, lp);
           }
           break;
         default:
-          atomicAdd(aw.lscatter + t, g1 * J->rc[0]);
+          atomicAdd(aw.lscatter + gidx(m, t, C), g1 * J->rc[0]);
           for (int q = 0; q < 3; ++q)
-            if (J->rc[1 + q] != 0.) atomicAdd(aw.lz + cnode(m, t, q), g1 * J->rc[1 + q]);
+            if (J->rc[1 + q] != 0.) atomicAdd(aw.lz + cnode(m, gidx(m, t, C), q), g1 * J->rc[1 + q]);
           break;
       }
     }
@@ -848,7 +851,7 @@ __global__ void __launch_bounds__(256) k_adj_recon(DevMesh m, DevWork wk, AdjWor
 __global__ void __launch_bounds__(32) k_pw_jacobian(DevMesh m, DevWork wk, AdjWork aw, const double* W) {
   const int n = min(*wk.pwcount, m.C);
   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
-    const int i = wk.pwlist[q];
+    const int i = gidx(m, wk.pwlist[q], m.C);
     pw_jacobian(m, wk, aw, W, i, aw.pwjac + i);
   }
 }

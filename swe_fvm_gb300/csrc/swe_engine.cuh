@@ -80,6 +80,9 @@ struct DevMesh {
   const int* inst_cell_begin;  // [I]
   const double* inst_cfl;      // [I]
   const double* inst_cor;      // [I]
+  // the engine's device error word (DevWork::err), for the range checks of
+  // checked builds in code that sees only the mesh
+  unsigned* err;
 };
 
 struct DevWork {
@@ -111,18 +114,20 @@ struct DevWork {
 // an index outside [0, n) sets kErrBadIndex and becomes 0, so the access stays
 // in bounds and the kernel's control flow (and its warp collectives) is
 // unchanged; the product build returns the index untouched.
-__device__ __forceinline__ int gidx(const DevWork& wk, int idx, int n) {
+__device__ __forceinline__ int gidx(unsigned* err, int idx, int n) {
 #ifdef SWE_CHECKED
   if ((unsigned)idx >= (unsigned)n) {
-    atomicOr(wk.err, kErrBadIndex);
+    atomicOr(err, kErrBadIndex);
     return 0;
   }
 #else
-  (void)wk;
+  (void)err;
   (void)n;
 #endif
   return idx;
 }
+__device__ __forceinline__ int gidx(const DevWork& wk, int idx, int n) { return gidx(wk.err, idx, n); }
+__device__ __forceinline__ int gidx(const DevMesh& m, int idx, int n) { return gidx(m.err, idx, n); }
 
 // One Runge-Kutta stage in Shu-Osher form (src/Solvers.cpp:5-59).
 struct Stage {

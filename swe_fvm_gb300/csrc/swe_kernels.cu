@@ -685,6 +685,7 @@ std::string Engine::init(std::vector<HostInstance>&& inst, int flux, int ws, int
   d_fixed_dt = dalloc<double>(I);  // per instance
   Wk.fixed_dt = d_fixed_dt;
   Wk.err = dalloc<unsigned>(1);
+  M.err = Wk.err;
   for (int q = 0; q < 6; ++q) state_[q] = dalloc<double>(C);
   d_io = dalloc<double>(3 * C);
   d_ioflag = dalloc<unsigned>(1);

@@ -37,6 +37,19 @@ def main():
     b.run_cfl(1, 15)
     b.synchronize()
     out["batch"] = [digest(b.prim(q)) for q in range(len(cases))]
+    # the discrete adjoint: traces exactly, gradients through sums whose
+    # atomic order may differ between runs (compared to round-off by the test)
+    from swe_fvm_gb300.adjoint import Rollout
+
+    m, prim = cases["bump"]
+    gauges = np.random.default_rng(4).choice(m.num_cells, 8, replace=False)
+    ro = Rollout(m, prim, cfl=0.3)
+    tr = ro.forward(1, 20, 8, gauges, 4)
+    gp, gz = ro.backward(np.ones_like(tr))
+    ro.sd.synchronize()
+    out["adjoint_traces"] = digest(tr)
+    out["adjoint_grads"] = [float(np.abs(gp).sum()), float(np.abs(gz).sum()), float(np.abs(gp).max()),
+                            float(np.abs(gz).max())]
     print(json.dumps(out))
     return 0
 

@@ -1,6 +1,8 @@
-"""The checked build (every gathered index of the step kernels range-checked
-on the device, a bad one setting an error bit instead of faulting) runs the
-same steps as the product build without raising and with the same bits."""
+"""The checked build (every gathered index of the step kernels and of the
+adjoint's reverse kernels range-checked on the device, a bad one setting an
+error bit instead of faulting) runs the same steps and the same adjoint as
+the product build without raising: the same bits for states and traces, the
+same gradients to round-off."""
 import json
 import os
 import subprocess
@@ -28,4 +30,7 @@ def test_checked_build_matches_the_product_build(gpu):
     a, b = _run(False), _run(True)
     assert not a.pop("checked") and b.pop("checked")
     assert a.pop("library") != b.pop("library")
+    ga, gb = a.pop("adjoint_grads"), b.pop("adjoint_grads")
     assert a == b
+    for x, y in zip(ga, gb):
+        assert x > 0 and abs(x - y) <= 1e-12 * x
