@@ -318,17 +318,19 @@ swe_status build_ctx(HostInstance&& h, swe::Layout&& L, const swe_params& p, con
   return SWE_OK;
 }
 
-// SWE_REORDER_AUTO on a large mesh: builds a context in each order (the
-// caller's, Morton, RCM), times kTimedLayoutSteps graph-replayed SSPRK2 steps
-// of each from the initial state (twice, keeping the faster), and keeps the
-// fastest; another order replaces the current best only when it is more than
-// 2 % faster.  At most two contexts exist at once, and a candidate is skipped
-// when the device has no room for it beside the best one.
-swe_status create_timed(const HostInstance& h, const swe_params& p, const double* prim0,
-                        std::unique_ptr<swe_ctx>* out, std::string* why) {
+// SWE_REORDER_AUTO on a large mesh or batch: builds the context (swe_ctx) or
+// batch (swe_batch) in each order (the caller's, Morton, RCM; a batch takes one
+// order for all its instances) through build(strategy, &candidate), times
+// kTimedLayoutSteps graph-replayed SSPRK2 steps of each from the initial state
+// (twice, keeping the faster), and keeps the fastest; another order replaces
+// the current best only when it is more than 2 % faster.  At most two exist at
+// once, and a candidate is skipped when the device has no room for it beside
+// the best one.
+template <class T, class Build>
+swe_status choose_timed(Build&& build, std::unique_ptr<T>* out, std::string* why) {
   Trace trace("swe_time_layouts");
   static const int kCand[3] = {SWE_REORDER_KEEP, SWE_REORDER_MORTON, SWE_REORDER_RCM};
-  std::unique_ptr<swe_ctx> best;
+  std::unique_ptr<T> best;
   float best_ms = 0.f;
   for (int s : kCand) {
     if (best) {
@@ -336,10 +338,8 @@ swe_status create_timed(const HostInstance& h, const swe_params& p, const double
       if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) break;
       if (free_b < best->eng.device_bytes() + best->eng.device_bytes() / 4 + (size_t(256) << 20)) break;
     }
-    swe::Layout L = swe::make_layout(h, s);
-    HostInstance d = L.identity() ? h : swe::apply_layout(h, L);
-    std::unique_ptr<swe_ctx> c;
-    swe_status st = build_ctx(std::move(d), std::move(L), p, prim0, &c, why);
+    std::unique_ptr<T> c;
+    swe_status st = build(s, &c);
     if (st != SWE_OK) {
       if (best) break;  // keep what already works
       return st;
@@ -360,6 +360,16 @@ swe_status create_timed(const HostInstance& h, const swe_params& p, const double
   }
   *out = std::move(best);
   return SWE_OK;
+}
+
+swe_status create_timed(const HostInstance& h, const swe_params& p, const double* prim0,
+                        std::unique_ptr<swe_ctx>* out, std::string* why) {
+  auto build = [&](int s, std::unique_ptr<swe_ctx>* c) {
+    swe::Layout L = swe::make_layout(h, s);
+    HostInstance d = L.identity() ? h : swe::apply_layout(h, L);
+    return build_ctx(std::move(d), std::move(L), p, prim0, c, why);
+  };
+  return choose_timed<swe_ctx>(build, out, why);
 }
 
 // A batch over validated instances already in the device orders of lay.
@@ -389,50 +399,21 @@ swe_status build_batch(std::vector<HostInstance>&& inst, std::vector<swe::Layout
   return SWE_OK;
 }
 
-// SWE_REORDER_AUTO for a batch of 65,536 cells or more: the same timed choice
-// as for a single context, over batches whose instances all take one order
-// (the callers', Morton, RCM).
+// SWE_REORDER_AUTO for a batch of 65,536 cells or more: choose_timed over
+// batches whose instances all take one order.
 swe_status create_batch_timed(const std::vector<HostInstance>& inst, const swe_params& p0, const double* const* prim0,
                               std::unique_ptr<swe_batch>* out, std::string* why) {
-  Trace trace("swe_time_layouts");
-  static const int kCand[3] = {SWE_REORDER_KEEP, SWE_REORDER_MORTON, SWE_REORDER_RCM};
-  const size_t n = inst.size();
-  std::unique_ptr<swe_batch> best;
-  float best_ms = 0.f;
-  for (int s : kCand) {
-    if (best) {
-      size_t free_b = 0, total_b = 0;
-      if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) break;
-      if (free_b < best->eng.device_bytes() + best->eng.device_bytes() / 4 + (size_t(256) << 20)) break;
-    }
+  auto build = [&](int s, std::unique_ptr<swe_batch>* c) {
+    const size_t n = inst.size();
     std::vector<HostInstance> d(n);
     std::vector<swe::Layout> L(n);
     for (size_t q = 0; q < n; ++q) {
       L[q] = swe::make_layout(inst[q], s);
       d[q] = L[q].identity() ? inst[q] : swe::apply_layout(inst[q], L[q]);
     }
-    std::unique_ptr<swe_batch> c;
-    swe_status st = build_batch(std::move(d), std::move(L), p0, prim0, &c, why);
-    if (st != SWE_OK) {
-      if (best) break;
-      return st;
-    }
-    float ms = 0.f, ms2 = 0.f;
-    cudaError_t e = c->eng.time_steps(1, kTimedLayoutSteps, &ms);
-    if (e == cudaSuccess) e = c->eng.time_steps(1, kTimedLayoutSteps, &ms2);
-    if (e != cudaSuccess) return cuda_fail(why, e, "timing a device order");
-    st = prime(c->eng, why);
-    if (st == SWE_OK && cudaStreamSynchronize(c->eng.stream()) != cudaSuccess)
-      st = cuda_fail(why, cudaGetLastError(), "priming flux pass");
-    if (st != SWE_OK) return st;
-    ms = std::min(ms, ms2);
-    if (!best || ms < 0.98f * best_ms) {
-      best = std::move(c);
-      best_ms = ms;
-    }
-  }
-  *out = std::move(best);
-  return SWE_OK;
+    return build_batch(std::move(d), std::move(L), p0, prim0, c, why);
+  };
+  return choose_timed<swe_batch>(build, out, why);
 }
 
 #define SWE_GUARD_BEGIN try {
