@@ -10,7 +10,12 @@ Names, argument meaning and error behaviour follow NikitaMatckevich/SWE_FVM:
   plugins of include/Fluxes.h:14-111 over the wave speeds of src/Fluxes.cpp:5-26,
 * ``SpaceDisc(fluxer, domain, v0, cor=0, tau=0)`` -- include/SpaceDisc.h:20-48,
 * ``TimeDisc(sd)`` with ``CFLdt()`` -- include/TimeDisc.h:4-23,
-* ``Solvers.Euler / SSPRK2 / SSPRK3(td, dt)`` -- include/Solvers.h:4-10.
+* ``Solvers.Euler / SSPRK2 / SSPRK3(td, dt)`` -- include/Solvers.h:4-10, and
+  ``Solvers.Custom`` for a caller's Shu-Osher table (``SpaceDisc.set_scheme``).
+
+Beyond the reference: ``Batch`` (many meshes per launch), the device order and
+block-size tuner (``reorder=``, ``block=``, ``tuning()``, ``layout_plan``),
+checkpoints (``save`` / ``restore``) and device-pointer state I/O.
 
 The reference raises DomainError / SolverError (include/Exceptions.h:4-10);
 here every failure is a ``SweError`` (a RuntimeError) carrying the library's
