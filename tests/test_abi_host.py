@@ -16,7 +16,8 @@ HEADER = os.path.join(ROOT, "include", "swe_fvm_gb300.h")
 
 
 def declared_symbols():
-    text = open(HEADER).read()
+    with open(HEADER) as f:
+        text = f.read()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
     return sorted(set(re.findall(r"\b(swe_[a-z0-9_]+)\s*\(", text)))
 

@@ -31,7 +31,7 @@ def _rank(rank, world, port, out):
 
 def test_two_replicas_report_the_slowest_rank():
     world = 2
-    with mp.Manager() as mgr:
+    with mp.get_context("spawn").Manager() as mgr:
         out = mgr.dict()
         mp.spawn(_rank, args=(world, _free_port(), out), nprocs=world, join=True)
         res = dict(out)
