@@ -1,9 +1,10 @@
 """Mesh ingestion and the reference's text outputs.
 
-- ``read_gmsh``: ASCII Gmsh meshes (format 2.2 or 4.1) to the reference's
-  topology (notebooks/mesher.py:3-69 reads them through the gmsh API; gmsh is
-  not needed here).  Triangles (element type 2) become cells; node z is the
-  bathymetry; every edge with one cell is a solid wall.
+- ``read_gmsh`` / ``write_gmsh``: Gmsh meshes (format 2.2 or 4.1, ASCII or
+  binary) to and from the reference's topology (notebooks/mesher.py:3-69 reads
+  them through the gmsh API; gmsh is not needed here).  Triangles (element
+  type 2) become cells; node z is the bathymetry; every edge with one cell is
+  a solid wall.
 - ``dump_fields``: (w, hu, hv) per cell, tab-separated
   (examples/Main.cpp:65-73, dumpFields).
 - ``dump_domain`` / ``load_domain``: node geometry and topology text files
@@ -15,13 +16,14 @@
 from __future__ import annotations
 
 import hashlib
+import struct
 from typing import NamedTuple
 
 import numpy as np
 
 from .mesh import Mesh, build_topology, load_reference_dump
 
-__all__ = ["read_gmsh", "dump_fields", "dump_domain", "load_domain", "save_state", "load_state",
+__all__ = ["read_gmsh", "write_gmsh", "dump_fields", "dump_domain", "load_domain", "save_state", "load_state",
            "mesh_fingerprint", "State"]
 
 
@@ -87,23 +89,117 @@ def _gmsh4(sec: dict):
     return np.array(tags, dtype=np.int64), np.array(coords).reshape(-1, 3), np.array(tris, dtype=np.int64).reshape(-1, 3)
 
 
-def read_gmsh(path: str, bathymetry=None) -> Mesh:
-    """ASCII Gmsh mesh -> Mesh.  bathymetry(x, y), if given, replaces the
-    node z.  Nodes not used by any triangle are dropped; the rest keep the
-    file's order."""
-    with open(path) as fh:
-        sec = _sections(fh.read())
-    if "MeshFormat" not in sec:
-        raise ValueError(f"{path}: no $MeshFormat section")
-    version, binary = sec["MeshFormat"][0].split()[:2]
-    if binary != "0":
-        raise ValueError(f"{path}: binary Gmsh files are not supported")
-    if version.startswith("2"):
-        tags, xyz, tris = _gmsh2(sec)
-    elif version.startswith("4"):
-        tags, xyz, tris = _gmsh4(sec)
+# nodes per element of the Gmsh element types a 2-D or 3-D mesh file may carry
+_NODES_PER_TYPE = {1: 2, 2: 3, 3: 4, 4: 4, 5: 8, 6: 6, 7: 5, 8: 3, 9: 6, 10: 9, 11: 10, 12: 27, 13: 18, 14: 14,
+                   15: 1, 16: 8, 17: 20, 18: 15, 19: 13, 20: 9, 21: 10, 22: 12, 23: 15, 24: 15, 25: 21, 26: 4,
+                   27: 5, 28: 6, 29: 20, 30: 35, 31: 56, 92: 64, 93: 125}
+
+
+def _binary_body(data: bytes, name: str, path: str) -> int:
+    """Offset of the first byte after the '$name' line."""
+    key = b"$" + name.encode() + b"\n"
+    at = data.find(key)
+    if at < 0:
+        raise ValueError(f"{path}: no ${name} section")
+    return at + len(key)
+
+
+def _gmsh_binary(data: bytes, version: str, dsize: int, path: str):
+    """Binary Gmsh 2.2 / 4.1: nodes (tags, xyz) and the triangles' node tags."""
+    pos = _binary_body(data, "MeshFormat", path)
+    pos = data.index(b"\n", pos) + 1  # the "version 1 size" line
+    if struct.unpack_from("<i", data, pos)[0] == 1:
+        e = "<"
+    elif struct.unpack_from(">i", data, pos)[0] == 1:
+        e = ">"
     else:
+        raise ValueError(f"{path}: unreadable binary header")
+    st = {4: "i4", 8: "i8"}.get(dsize)
+    if st is None:
+        raise ValueError(f"{path}: data size {dsize} is not supported")
+    st, i4, f8 = np.dtype(e + st), np.dtype(e + "i4"), np.dtype(e + "f8")
+    if version.startswith("4"):
+        pos = _binary_body(data, "Nodes", path)
+        n_blocks = int(np.frombuffer(data, st, 4, pos)[0])
+        pos += 4 * dsize
+        tags, coords = [], []
+        for _ in range(n_blocks):
+            dim, _tag, parametric = (int(v) for v in np.frombuffer(data, i4, 3, pos))
+            count = int(np.frombuffer(data, st, 1, pos + 12)[0])
+            pos += 12 + dsize
+            tags.append(np.frombuffer(data, st, count, pos).astype(np.int64))
+            pos += count * dsize
+            width = 3 + (dim if parametric else 0)
+            coords.append(np.frombuffer(data, f8, count * width, pos).reshape(count, width)[:, :3])
+            pos += count * width * 8
+        pos = _binary_body(data, "Elements", path)
+        n_blocks = int(np.frombuffer(data, st, 4, pos)[0])
+        pos += 4 * dsize
+        tris = []
+        for _ in range(n_blocks):
+            _dim, _tag, etype = (int(v) for v in np.frombuffer(data, i4, 3, pos))
+            count = int(np.frombuffer(data, st, 1, pos + 12)[0])
+            pos += 12 + dsize
+            if etype not in _NODES_PER_TYPE:
+                raise ValueError(f"{path}: element type {etype} is not supported")
+            width = 1 + _NODES_PER_TYPE[etype]
+            rows = np.frombuffer(data, st, count * width, pos).reshape(count, width)
+            if etype == 2:
+                tris.append(rows[:, 1:4].astype(np.int64))
+            pos += count * width * dsize
+        xyz = np.concatenate(coords) if coords else np.zeros((0, 3))
+        tags = np.concatenate(tags) if tags else np.zeros(0, np.int64)
+        tris = np.concatenate(tris) if tris else np.zeros((0, 3), np.int64)
+        return tags, xyz, tris
+    # 2.2: the counts are text lines, the records binary
+    pos = _binary_body(data, "Nodes", path)
+    end = data.index(b"\n", pos)
+    n = int(data[pos:end])
+    rec = np.dtype([("tag", i4), ("xyz", f8, (3,))])
+    nodes = np.frombuffer(data, rec, n, end + 1)
+    pos = _binary_body(data, "Elements", path)
+    end = data.index(b"\n", pos)
+    remaining = int(data[pos:end])
+    pos = end + 1
+    tris = []
+    while remaining > 0:
+        etype, count, ntags = (int(v) for v in np.frombuffer(data, i4, 3, pos))
+        pos += 12
+        if etype not in _NODES_PER_TYPE or count <= 0:
+            raise ValueError(f"{path}: bad element block (type {etype}, {count} elements)")
+        width = 1 + ntags + _NODES_PER_TYPE[etype]
+        rows = np.frombuffer(data, i4, count * width, pos).reshape(count, width)
+        if etype == 2:
+            tris.append(rows[:, 1 + ntags:4 + ntags].astype(np.int64))
+        pos += count * width * 4
+        remaining -= count
+    tris = np.concatenate(tris) if tris else np.zeros((0, 3), np.int64)
+    return nodes["tag"].astype(np.int64), np.array(nodes["xyz"], dtype=np.float64), tris
+
+
+def read_gmsh(path: str, bathymetry=None) -> Mesh:
+    """Gmsh mesh (format 2.2 or 4.1, ASCII or binary) -> Mesh.  bathymetry(x,
+    y), if given, replaces the node z.  Nodes not used by any triangle are
+    dropped; the rest keep the file's order."""
+    with open(path, "rb") as fh:
+        data = fh.read()
+    head = data[:256].decode("latin-1")
+    if "$MeshFormat" not in head:
+        raise ValueError(f"{path}: no $MeshFormat section")
+    fmt = head.split("$MeshFormat", 1)[1].split()
+    if len(fmt) < 3:
+        raise ValueError(f"{path}: malformed $MeshFormat")
+    version, binary, dsize = fmt[0], fmt[1], int(fmt[2])
+    if not (version.startswith("2") or version.startswith("4")):
         raise ValueError(f"{path}: Gmsh format {version} is not supported (2.2 or 4.1)")
+    if binary != "0":
+        try:
+            tags, xyz, tris = _gmsh_binary(data, version, dsize, path)
+        except (IndexError, ValueError, struct.error) as ex:
+            raise ValueError(f"{path}: {ex}") from None
+    else:
+        sec = _sections(data.decode("latin-1"))
+        tags, xyz, tris = (_gmsh2 if version.startswith("2") else _gmsh4)(sec)
     if len(tris) == 0:
         raise ValueError(f"{path}: no triangles")
     index = {int(t): k for k, t in enumerate(tags)}
@@ -115,6 +211,51 @@ def read_gmsh(path: str, bathymetry=None) -> Mesh:
     if bathymetry is not None:
         pts[:, 2] = bathymetry(pts[:, 0], pts[:, 1])
     return build_topology(pts, remap[tri])
+
+
+def write_gmsh(path: str, mesh: Mesh, version: str = "4.1", binary: bool = False) -> None:
+    """The mesh as a Gmsh file (format 2.2 or 4.1, ASCII or binary): its nodes
+    (x, y, z with z the bathymetry, tags 1..N) and its triangles (tags 1..C),
+    one block each, little-endian 8-byte sizes when binary."""
+    xyz = np.ascontiguousarray(mesh.geometry, dtype="<f8")
+    tri = np.ascontiguousarray(mesh.cell_nodes, dtype=np.int64) + 1
+    N, C = len(xyz), len(tri)
+    v4 = version.startswith("4")
+    with open(path, "wb") as fh:
+        fh.write(f"$MeshFormat\n{'4.1' if v4 else '2.2'} {1 if binary else 0} 8\n".encode())
+        if binary:
+            fh.write(np.array([1], "<i4").tobytes() + b"\n")
+        fh.write(b"$EndMeshFormat\n$Nodes\n")
+        if v4 and binary:
+            fh.write(np.array([1, N, 1, N], "<u8").tobytes() + np.array([2, 1, 0], "<i4").tobytes()
+                     + np.array([N], "<u8").tobytes() + np.arange(1, N + 1, dtype="<u8").tobytes() + xyz.tobytes())
+        elif v4:
+            fh.write(f"1 {N} 1 {N}\n2 1 0 {N}\n".encode())
+            fh.write("".join(f"{k}\n" for k in range(1, N + 1)).encode())
+            fh.write("".join(f"{float(x)!r} {float(y)!r} {float(z)!r}\n" for x, y, z in xyz).encode())
+        elif binary:
+            rec = np.zeros(N, np.dtype([("tag", "<i4"), ("xyz", "<f8", (3,))]))
+            rec["tag"], rec["xyz"] = np.arange(1, N + 1), xyz
+            fh.write(f"{N}\n".encode() + rec.tobytes())
+        else:
+            fh.write(f"{N}\n".encode())
+            fh.write("".join(f"{k + 1} {float(x)!r} {float(y)!r} {float(z)!r}\n"
+                             for k, (x, y, z) in enumerate(xyz)).encode())
+        fh.write(b"\n$EndNodes\n$Elements\n" if binary else b"$EndNodes\n$Elements\n")
+        ids = np.arange(1, C + 1, dtype=np.int64)
+        if v4 and binary:
+            fh.write(np.array([1, C, 1, C], "<u8").tobytes() + np.array([2, 1, 2], "<i4").tobytes()
+                     + np.array([C], "<u8").tobytes() + np.column_stack([ids, tri]).astype("<u8").tobytes())
+        elif v4:
+            fh.write(f"1 {C} 1 {C}\n2 1 2 {C}\n".encode())
+            fh.write("".join(f"{i} {a} {b} {c}\n" for i, (a, b, c) in zip(ids, tri)).encode())
+        elif binary:
+            body = np.column_stack([ids, np.ones(C, np.int64), tri]).astype("<i4")  # id, physical tag, nodes
+            fh.write(f"{C}\n".encode() + np.array([2, C, 1], "<i4").tobytes() + body.tobytes())
+        else:
+            fh.write(f"{C}\n".encode())
+            fh.write("".join(f"{i} 2 1 1 {a} {b} {c}\n" for i, (a, b, c) in zip(ids, tri)).encode())
+        fh.write(b"\n$EndElements\n" if binary else b"$EndElements\n")
 
 
 def dump_fields(mesh: Mesh, prim, path: str) -> None:

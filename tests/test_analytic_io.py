@@ -1,4 +1,4 @@
-"""Mesh ingestion (Gmsh 2.2 / 4.1 ASCII), the reference's text outputs, and the
+"""Mesh ingestion (Gmsh 2.2 / 4.1, ASCII and binary), the reference's text outputs, and the
 closed-form solutions of the test layer (CPU only)."""
 import math
 
@@ -78,9 +78,50 @@ def test_read_gmsh_bathymetry_override(tmp_path):
     assert np.allclose(m.geometry[:, 2], m.geometry[:, 0] * m.geometry[:, 1])
 
 
-def test_read_gmsh_rejects_binary(tmp_path):
+@pytest.mark.parametrize("version", ["4.1", "2.2"])
+@pytest.mark.parametrize("binary", [False, True])
+def test_write_and_read_gmsh_round_trip(tmp_path, version, binary):
+    m = structured_square(7, 0.0, 2.0, bathymetry=lambda x, y: 0.1 * x - 0.2 * y * y)
+    p = tmp_path / "m.msh"
+    fileio.write_gmsh(str(p), m, version, binary)
+    _same_mesh(fileio.read_gmsh(str(p)), m.contiguous())
+
+
+def _write_gmsh41_binary(path, xyz, tri, endian="<"):
+    # a point block with an unused node, a surface node block, a line block
+    # and a triangle block, like a file Gmsh writes for a 2-D model
+    u8, i4, f8 = endian + "u8", endian + "i4", endian + "f8"
+    n = len(xyz)
+    parts = [b"$MeshFormat\n4.1 1 8\n", np.array([1], i4).tobytes(), b"\n$EndMeshFormat\n$Nodes\n"]
+    parts += [np.array([2, n + 1, 1, n + 1], u8).tobytes()]
+    parts += [np.array([0, 7, 0], i4).tobytes(), np.array([1, n + 1], u8).tobytes(),
+              np.array([9.0, 9.0, 0.0], f8).tobytes()]
+    parts += [np.array([2, 1, 0], i4).tobytes(), np.array([n], u8).tobytes(),
+              np.arange(1, n + 1, dtype=u8).tobytes(), np.asarray(xyz, f8).tobytes()]
+    parts += [b"\n$EndNodes\n$Elements\n", np.array([2, len(tri) + 1, 1, len(tri) + 1], u8).tobytes()]
+    parts += [np.array([1, 3, 1], i4).tobytes(), np.array([1], u8).tobytes(), np.array([1, 1, 2], u8).tobytes()]
+    ids = np.arange(2, len(tri) + 2)
+    parts += [np.array([2, 1, 2], i4).tobytes(), np.array([len(tri)], u8).tobytes(),
+              np.column_stack([ids, np.asarray(tri) + 1]).astype(u8).tobytes(), b"\n$EndElements\n"]
+    path.write_bytes(b"".join(parts))
+
+
+@pytest.mark.parametrize("endian", ["<", ">"])
+def test_read_binary_gmsh41_with_other_blocks(tmp_path, endian):
+    xyz, tri = _grid(5)
     p = tmp_path / "b.msh"
-    p.write_text("$MeshFormat\n4.1 1 8\n$EndMeshFormat\n")
+    _write_gmsh41_binary(p, xyz, tri, endian)
+    _same_mesh(fileio.read_gmsh(str(p)), build_topology(xyz, tri))
+
+
+def test_read_gmsh_rejects_truncated_binary(tmp_path):
+    xyz, tri = _grid(4)
+    p = tmp_path / "b.msh"
+    _write_gmsh41_binary(p, xyz, tri)
+    p.write_bytes(p.read_bytes()[:-200])
+    with pytest.raises(ValueError):
+        fileio.read_gmsh(str(p))
+    p.write_text("$MeshFormat\n3.0 0 8\n$EndMeshFormat\n")
     with pytest.raises(ValueError):
         fileio.read_gmsh(str(p))
 
