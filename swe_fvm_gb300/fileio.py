@@ -202,8 +202,16 @@ def read_gmsh(path: str, bathymetry=None) -> Mesh:
         tags, xyz, tris = (_gmsh2 if version.startswith("2") else _gmsh4)(sec)
     if len(tris) == 0:
         raise ValueError(f"{path}: no triangles")
-    index = {int(t): k for k, t in enumerate(tags)}
-    tri = np.vectorize(lambda t: index[int(t)], otypes=[np.int64])(tris)
+    # node tag -> position in the file, vectorised
+    tags = np.asarray(tags, dtype=np.int64)
+    if len(tags) == 0:
+        raise ValueError(f"{path}: no nodes")
+    order = np.argsort(tags, kind="stable")
+    at = np.searchsorted(tags[order], tris)
+    at = np.minimum(at, len(tags) - 1)
+    tri = order[at]
+    if not np.array_equal(tags[tri], tris):
+        raise ValueError(f"{path}: a triangle names a node tag the file does not define")
     used = np.unique(tri)
     remap = -np.ones(len(tags), dtype=np.int64)
     remap[used] = np.arange(len(used))

@@ -223,3 +223,13 @@ def test_checkpoint_round_trip_is_bitwise_and_mesh_bound(tmp_path):
     other, _ = scenarios.random_front_case(10, 2)
     with pytest.raises(ValueError):
         load_state(str(tmp_path / "ck.npz"), other)
+
+
+def test_read_gmsh_rejects_an_undefined_node_tag(tmp_path):
+    xyz, tri = _grid(3)
+    tri = tri.copy()
+    tri[0, 1] = len(xyz) + 40  # no such node
+    p = tmp_path / "m.msh"
+    _write_gmsh22(p, xyz, tri)
+    with pytest.raises(ValueError, match="node tag"):
+        fileio.read_gmsh(str(p))
