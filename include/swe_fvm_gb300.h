@@ -262,9 +262,14 @@ swe_status swe_layout_plan(const swe_mesh* mesh, int32_t strategy, int64_t* cell
  *
  * Scratch lives in a static 512 KB device array held by every GPU that loads
  * this library, so n_edges is limited to 16,777,216 (larger requests return
- * SWE_ERR_INVALID_ARGUMENT).  The first call on a device looks up that array's
- * device address (make it before any stream capture).  All calls share the
- * array: calls that overlap on the GPU (other streams, other threads) race. */
+ * SWE_ERR_INVALID_ARGUMENT).  Every call looks up that array's address in the
+ * calling thread's current context (so a context switch or a device reset
+ * leaves no stale address); the first call in a context also loads the
+ * library's device code there, so make it before any stream capture.  All
+ * calls share the array: calls that overlap on the GPU (other streams, other
+ * threads) race.  An error already pending on the thread is returned as
+ * SWE_ERR_CUDA before anything is launched and is left pending; otherwise
+ * SWE_ERR_CUDA reports a failure of this call's own launches. */
 swe_status swe_edge_fluxes_noalloc(int32_t flux, int32_t wavespeed, int64_t n_edges, const double* edge_geom,
                                    const double* left, const double* right, double cor, double* flux_out,
                                    double* ratio_out, void* stream);

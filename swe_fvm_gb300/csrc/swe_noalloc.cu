@@ -11,8 +11,6 @@
 // holds until the process exits.
 #include <cuda_runtime.h>
 
-#include <mutex>
-
 #include "../../include/swe_fvm_gb300.h"
 #include "swe_physics.cuh"
 
@@ -81,24 +79,17 @@ __global__ void __launch_bounds__(kThreads) k_min_noalloc(int nblocks, const dou
   }
 }
 
-// Device address of g_block_min, looked up once per device with that device
-// current (host code may not use the symbol's name as a device pointer).
-std::mutex g_mu;
-double* g_addr[64] = {};
-
+// Device address of g_block_min in the calling thread's current context.  A
+// module-scope array has one address per context (and a new one after
+// cudaDeviceReset), so no address is cached: cudaGetSymbolAddress is a
+// host-side lookup that issues no stream work.  On the first call in a
+// context it also loads this library's device code into that context, which
+// is why that first call must come before any stream capture.
 cudaError_t scratch_address(double** out) {
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
+  void* p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_block_min);
   if (e != cudaSuccess) return e;
-  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
-  std::lock_guard<std::mutex> lock(g_mu);
-  if (!g_addr[dev]) {
-    void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_block_min);
-    if (e != cudaSuccess) return e;
-    g_addr[dev] = (double*)p;
-  }
-  *out = g_addr[dev];
+  *out = (double*)p;
   return cudaSuccess;
 }
 
@@ -118,6 +109,9 @@ extern "C" swe_status swe_edge_fluxes_noalloc(int32_t flux, int32_t wavespeed, i
   if (flux < 0 || flux > 1 || wavespeed < 0 || wavespeed > 2) return SWE_ERR_INVALID_ARGUMENT;
   if (n_edges <= 0 || n_edges > kMaxEdges) return SWE_ERR_INVALID_ARGUMENT;
   if (!edge_geom || !left || !right || !flux_out || !ratio_out) return SWE_ERR_INVALID_ARGUMENT;
+  // An error left pending by earlier work on this thread is reported as such
+  // (and left pending) instead of being consumed and blamed on these launches.
+  if (cudaPeekAtLastError() != cudaSuccess) return SWE_ERR_CUDA;
   double* scratch = nullptr;
   if (scratch_address(&scratch) != cudaSuccess) return SWE_ERR_CUDA;
   cudaStream_t s = (cudaStream_t)stream;

@@ -13,7 +13,9 @@ import sys
 
 import numpy as np
 
-root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+if len(sys.argv) != 2:
+    sys.exit("usage: python tests/golden/make_bowl_fixture.py <reference root>")
+root = sys.argv[1]
 nb = os.path.join(root, "notebooks")
 geo = np.loadtxt(os.path.join(nb, "geometry.dat")).reshape(-1, 3)
 lines = open(os.path.join(nb, "topology.dat")).read().split("\n")

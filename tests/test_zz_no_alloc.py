@@ -50,11 +50,9 @@ def edge_geometry(m):
     return np.ascontiguousarray(np.stack([t1, -t0, t0, t1, b, lmin], axis=1))
 
 
-@pytest.mark.parametrize("flux,ws", [(1, 2), (0, 2), (1, 0)])
-def test_noalloc_flux_pass_matches_context(gpu, flux, ws):
+def _run_case(m, prim, flux, ws):
     import torch
 
-    m, prim = scenarios.random_front_case(40, seed=11)
     fluxer = Fluxes.HLLC(ws) if flux == 1 else Fluxes.HLL(ws)
     sd = SpaceDisc(fluxer, m, prim)
     sd.ComputeInterfaceValues()
@@ -75,16 +73,38 @@ def test_noalloc_flux_pass_matches_context(gpu, flux, ws):
     d_flux = torch.full((len(interior), 3), float("nan"), dtype=torch.float64, device=dev)
     d_ratio = torch.zeros(1, dtype=torch.float64, device=dev)
     L = _lib.load()
+    free = []
     for call in range(2):
         d_flux.fill_(float("nan"))
         d_ratio.fill_(-1.0)
+        torch.cuda.synchronize()
+        free.append(torch.cuda.mem_get_info()[0])
         st = L.swe_edge_fluxes_noalloc(flux, ws, len(interior), d_geom.data_ptr(), d_left.data_ptr(),
                                        d_right.data_ptr(), 0.0, d_flux.data_ptr(), d_ratio.data_ptr(), None)
         assert st == 0
         torch.cuda.synchronize()
+        free.append(torch.cuda.mem_get_info()[0])
         f = d_flux.cpu().numpy()
         assert rel_l2(f, f_ref[interior]) <= TOL, call
         assert float(d_ratio.item()) == pytest.approx(r_ref, rel=TOL), call
+    # the second call (after the first has loaded the module into this
+    # context) leaves the device's free memory exactly as it found it
+    assert free[3] == free[2]
+    return len(interior)
+
+
+@pytest.mark.parametrize("flux,ws", [(1, 2), (0, 2), (1, 0)])
+def test_noalloc_flux_pass_matches_context(gpu, flux, ws):
+    m, prim = scenarios.random_front_case(40, seed=11)
+    _run_case(m, prim, flux, ws)
+
+
+def test_noalloc_many_blocks_matches_context(gpu):
+    """More than 256 blocks of partial minima (over 65,536 interior edges), so
+    every thread of the folding block reads several partial minima."""
+    m, prim = scenarios.random_front_case(200, seed=5)
+    n = _run_case(m, prim, 1, 2)
+    assert n > 65536
 
 
 def test_noalloc_rejects_sizes_beyond_the_scratch(gpu):
