@@ -362,7 +362,7 @@ __device__ double pass1_node_value(const DevMesh& m, const DevWork& wk, const do
   const P1 p = pass1(wk, W, c);
   if (p.type == 0) return m.dry[(size_t)c * kDryStride + kn];
   double off = 0.;
-  if (p.type == 2 && p.kept) off = m.combo[((size_t)c * 8 + p.mask) * kComboStride + 8 + kn];
+  if (p.type == 2 && p.kept) off = m.combo[combo_off(m.C, c, p.mask) + 8 + kn];
   const double a = p.w0 + off;
   return dge0(a - z) ? a : z;
 }
@@ -656,7 +656,7 @@ __device__ void pw_jacobian(const DevMesh& m, const DevWork& wk, const AdjWork& 
       }
     } else {
       double off_n = 0.;
-      if (pc.type == 2 && pc.kept) off_n = m.combo[((size_t)best * 8 + pc.mask) * kComboStride + 8 + bestk];
+      if (pc.type == 2 && pc.kept) off_n = m.combo[combo_off(m.C, best, pc.mask) + 8 + bestk];
       if (dge0((pc.w0 + off_n) - zc_)) {
         J.target = best;
         if (pc.type == 2) {
@@ -746,7 +746,7 @@ __device__ void adj_recon_cell(const DevMesh& m, const DevWork& wk, AdjWork aw, 
   const PwJac* J = nullptr;
   if (p.type == 2) {
     if (p.kept) {
-      const double* rec = m.combo + ((size_t)i * 8 + p.mask) * kComboStride;
+      const double* rec = m.combo + combo_off(m.C, i, p.mask);
       gx = rec[0];
       gy = rec[1];
       for (int k = 0; k < 3; ++k) off[k] = rec[5 + k];

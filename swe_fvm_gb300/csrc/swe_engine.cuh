@@ -26,6 +26,27 @@ constexpr int kDryStride = 8;     // doubles per dry-cell record
 
 enum : unsigned { kErrNonFinite = 1u, kErrBadState = 2u, kErrBadIndex = 4u };
 
+// The full-wet combination records are stored combination-major, [8][C][12]:
+// the record of cell i for neighbour combination `mask` starts here.  Nearly
+// every fully-wet cell has only fully-wet neighbours (mask 0), so the records
+// a warp reads are contiguous.
+__host__ __device__ __forceinline__ size_t combo_off(int C, int i, int mask) {
+  return ((size_t)mask * (size_t)C + (size_t)i) * kComboStride;
+}
+
+// Static per-slot record read by the update kernel with two 16-byte loads:
+// L(e_k) / A, the edge-centre bathymetry and the normal times L(e_k) / A.
+struct __align__(16) SlotRec {
+  double cek, ze, nxc, nyc;
+};
+
+// Static per-edge record read by the flux kernel with three 16-byte loads:
+// the owner's outward normal and tangent, the edge-centre bathymetry and
+// min(2 A_owner / L, 2 A_neighbour / L).
+struct __align__(16) EdgeRec {
+  double nx, ny, tx, ty, b, lmin;
+};
+
 // PartWet2 (src/MUSCLObject.cpp:114-191) geometry: vertices sorted by z.
 struct Pw2Rec {
   double p[3][3];     // sorted vertices (x, y, z), lowest first
@@ -58,10 +79,12 @@ struct DevMesh {
   const double* cnxc;         // [3][C] outward normal of edge k times L_k / A (x)
   const double* cnyc;         // [3][C] (y)
   const double* dry;          // [C][8] dry-cell node/edge values and slope
-  const double* combo;        // [C][8][12] full-wet plane records
+  const double* combo;        // [8][C][12] full-wet plane records (combo_off)
   const double* pw1;          // [C][12]
   const Pw2Rec* pw2;          // [C]
   const int* cinst;           // [C] instance of the cell (batched only)
+  const SlotRec* srec;        // [3][C] cek, ze, cnxc, cnyc of each slot, packed
+  const int2* cslot;          // [3][C] (cedge, cnbr) of each slot, packed
   // edges
   const int* eown;    // [E]
   const int* enb;     // [E] -1 = wall
@@ -74,6 +97,8 @@ struct DevMesh {
   const double* ezm;    // edge-centre bathymetry
   const double* elmin;  // min(2A_owner/L, 2A_nb/L)
   const int* einst;     // [E] (batched only)
+  const EdgeRec* erec;  // [E] enx, eny, etx, ety, ezm, elmin, packed
+  const int4* eidx;     // [E] (eown, enb, eslotl, eslotr), packed
   // nodes
   const double* nz;  // [N]
   // instances
@@ -325,6 +350,10 @@ struct HostImage {
   std::vector<double> bc, fwthr, area, zn, ze, cek, cnxc, cnyc, dry, combo, pw1, enx, eny, etx, ety, ezm, elmin, nz,
       inst_cfl, inst_cor;
   std::vector<Pw2Rec> pw2;
+  std::vector<SlotRec> srec;
+  std::vector<int2> cslot;
+  std::vector<EdgeRec> erec;
+  std::vector<int4> eidx;
   void resize(int C_, int E_, int N_, int I_);
 };
 std::string validate_instance(const HostInstance& h);

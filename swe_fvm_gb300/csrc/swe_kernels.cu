@@ -55,6 +55,18 @@ constexpr double kInf = __builtin_huge_val();
 
 __device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }
 
+// start moving the cache line of p towards this SM's L1 (no register, no wait)
+__device__ __forceinline__ void prefetch_l1(const void* p) {
+  asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
+}
+
+// two 16-byte loads of a 32-byte record through the read-only path
+__device__ __forceinline__ void ldg_pair(const void* p, double2* a, double2* b) {
+  const double2* q = (const double2*)p;
+  *a = __ldg(q);
+  *b = __ldg(q + 1);
+}
+
 // ------------------------------------------------------------ interface write
 // UpdateInterfaceValues for one edge slot (src/SpaceDisc.cpp:24-29): AtPoint
 // value (w, u, v) already dry-checked, through PrimAssigner with the edge
@@ -123,7 +135,7 @@ __device__ __forceinline__ double partwet1_level(const double* __restrict__ p, d
 
 // ---------------------------------------------------------------- kernels
 template <bool BATCH, bool COR0>
-__global__ void __launch_bounds__(256) k_recon1(DevMesh m, DevWork wk, const double* __restrict__ W,
+__global__ void __launch_bounds__(256, 5) k_recon1(DevMesh m, DevWork wk, const double* __restrict__ W,
                                                 const double* __restrict__ U, const double* __restrict__ V,
                                                 int latch_mode) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -144,6 +156,11 @@ __global__ void __launch_bounds__(256) k_recon1(DevMesh m, DevWork wk, const dou
       wk.r[inst] = order_key(1.0);  // src/SpaceDisc.cpp:56
     }
     const int C = m.C;
+    // the combination record of the all-fully-wet neighbourhood (mask 0) is
+    // the one nearly every fully-wet cell reads: start its lines towards L1
+    // now, before the loads that decide the class and the mask
+    prefetch_l1(m.combo + combo_off(C, i, 0));
+    prefetch_l1(m.combo + combo_off(C, i, 0) + 8);
     const double cor = m.inst_cor[inst];
     const double w = W[i], u = U[i], v = V[i];
     const double h = w - m.bc[i];
@@ -192,7 +209,7 @@ __global__ void __launch_bounds__(256) k_recon1(DevMesh m, DevWork wk, const dou
       double gx = 0., gy = 0.;
       double toff[3] = {0., 0., 0.}, noff[3] = {0., 0., 0.};
       if (!first_order) {
-        const double* rec = m.combo + ((size_t)i * 8 + mask) * kComboStride;
+        const double* rec = m.combo + combo_off(C, i, mask);
         const double g0 = rec[0], g1 = rec[1];
         bool pos = true;
 #pragma unroll
@@ -331,20 +348,24 @@ __global__ void __launch_bounds__(256) k_recon2(DevMesh m, DevWork wk, const dou
 template <class FLUX, bool TAPE>
 __device__ __forceinline__ void flux_edge(const DevMesh& m, const DevWork& wk, const double* __restrict__ W, int e,
                                           int inst, double* lw) {
-  const int o = gidx(wk, m.eown[e], m.C);
-  const int nb = m.enb[e];
+  const int4 ix = __ldg(m.eidx + e);  // (owner, neighbour, owner's slot, neighbour's slot)
+  const int o = gidx(wk, ix.x, m.C);
+  const int nb = ix.y;
   double F[3];
-  const double nx = m.enx[e], ny = m.eny[e];
+  const double2* gr = (const double2*)(m.erec + e);
+  const double2 n2 = __ldg(gr);
+  const double nx = n2.x, ny = n2.y;
   if (nb < 0) {
     // solid wall: ElemFlux with the owner's cell-average depth (src/SpaceDisc.cpp:66-69)
     elem_flux(nx, ny, W[o] - m.bc[o], 0., 0., F);
   } else {
+    const double2 t2 = __ldg(gr + 1), bl = __ldg(gr + 2);
     EdgeGeom g;
     g.nx = nx; g.ny = ny;
-    g.tx = m.etx[e]; g.ty = m.ety[e];
-    g.b = m.ezm[e];
-    g.lmin = m.elmin[e];
-    const int sl = gidx(wk, m.eslotl[e], 3 * m.C), sr = gidx(wk, m.eslotr[e], 3 * m.C);
+    g.tx = t2.x; g.ty = t2.y;
+    g.b = bl.x;
+    g.lmin = bl.y;
+    const int sl = gidx(wk, ix.z, 3 * m.C), sr = gidx(wk, ix.w, 3 * m.C);
     SideState L{wk.ew[sl], wk.eu[sl], wk.ev[sl]};
     SideState R{wk.ew[sr], wk.eu[sr], wk.ev[sr]};
     if (TAPE) FLUX::eval(g, L, R, m.inst_cor[inst], lw, F, EdgeTape{wk.ftape, m.E, e});
@@ -358,8 +379,13 @@ __device__ __forceinline__ void flux_edge(const DevMesh& m, const DevWork& wk, c
 // MODE 0: every edge.  MODE 1: the edges none of whose cells is partially
 // wet (the others wait for PartWet2 and go through k_flux_pw).
 // TAPE: also store the intermediates the adjoint's reverse reads (wk.ftape).
+// Register caps (the second __launch_bounds__ argument: blocks of 256 threads
+// per SM) measured on the 1M-cell dam break, CUDA events, same bits: k_flux at
+// 64 registers 0.211 -> 0.199 ms per launch, k_recon1 at 48 registers
+// 0.091 -> 0.087 ms; more resident warps hide the gathers better than the
+// few spilled registers cost.
 template <class FLUX, bool BATCH, int MODE, bool TAPE>
-__global__ void __launch_bounds__(256) k_flux(DevMesh m, DevWork wk, const double* __restrict__ W) {
+__global__ void __launch_bounds__(256, 4) k_flux(DevMesh m, DevWork wk, const double* __restrict__ W) {
   __shared__ unsigned long long s_min[32];
   __shared__ int s_inst[32];
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
@@ -471,7 +497,7 @@ __global__ void __launch_bounds__(256) k_drain(DevMesh m, DevWork wk, const doub
 // HALF: a stage with a = b = c = 1/2 (SSPRK2's second), whose products with
 // the coefficients are exact halvings.
 template <bool BATCH, bool STORE_N, bool HALF>
-__global__ void __launch_bounds__(256) k_update(DevMesh m, DevWork wk, const double* Wp, const double* Up,
+__global__ void __launch_bounds__(256, 5) k_update(DevMesh m, DevWork wk, const double* Wp, const double* Up,
                                                 const double* Vp, const double* W0, const double* U0,
                                                 const double* V0, double* Wo, double* Uo, double* Vo, Stage st,
                                                 double* nst = nullptr) {
@@ -486,15 +512,18 @@ __global__ void __launch_bounds__(256) k_update(DevMesh m, DevWork wk, const dou
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
     const int slot = k * C + i;
-    const int e = gidx(wk, m.cedge[slot], m.E);
+    const int2 en = __ldg(m.cslot + slot);  // (edge, neighbour)
+    double2 ce, nc;                         // (L/A, edge-centre z), (n_x L/A, n_y L/A)
+    ldg_pair(m.srec + slot, &ce, &nc);
+    const int e = gidx(wk, en.x, m.E);
     // sgn = +1 for the edge's owner, else -1: products with it are sign changes
     const bool out = (own >> k) & 1u;
     const double F0 = wk.f0[e], F1 = wk.f1[e], F2 = wk.f2[e];
-    const int nb = m.cnbr[slot];
+    const int nb = en.y;
     const double dtik = nb < 0 ? kInf : wk.drain[gidx(wk, nb, C)];
     const double dtk = (out ? dgt0(F0) : dlt(F0, 0.)) ? smin(dt, dti) : smin(dt, dtik);  // sgn F0 > 0
-    const double c_ek = m.cek[slot];
-    const double h_ek = wk.ew[slot] - m.ze[slot];
+    const double c_ek = ce.x;
+    const double h_ek = wk.ew[slot] - ce.y;
     const double s = (out ? dtk : SWE_NEG(dtk)) * c_ek;
     r0 -= s * F0;
     r1 -= s * F1;
@@ -503,8 +532,8 @@ __global__ void __launch_bounds__(256) k_update(DevMesh m, DevWork wk, const dou
     r1 -= q * wk.sx[slot] * h_ek;
     r2 -= q * wk.sy[slot] * h_ek;
     const double p = SWE_HALF(h_ek) * h_ek;  // 0.5 h h
-    r1 += dtk * (m.cnxc[slot] * p);        // (n_x c) p
-    r2 += dtk * (m.cnyc[slot] * p);
+    r1 += dtk * (nc.x * p);  // (n_x c) p
+    r2 += dtk * (nc.y * p);
   }
   const double b = m.bc[i];
   const double h0 = W0[i] - b;
@@ -649,6 +678,10 @@ std::string Engine::init(std::vector<HostInstance>&& inst, int flux, int ws, int
   const double *p_bc, *p_fw, *p_area, *p_zn, *p_ze, *p_cek, *p_cnxc, *p_cnyc, *p_dry, *p_combo, *p_pw1, *p_enx, *p_eny,
       *p_etx, *p_ety, *p_ezm, *p_elmin, *p_nz, *p_cfl, *p_cor;
   const Pw2Rec* p_pw2;
+  const SlotRec* p_srec;
+  const int2* p_cslot;
+  const EdgeRec* p_erec;
+  const int4* p_eidx;
   ok = ok && up(img.cnode, p_cnode) && up(img.cnbr, p_cnbr) && up(img.cedge, p_cedge) && up(img.cinst, p_cinst);
   ok = ok && up(img.cown, p_cown) && up(img.bc, p_bc) && up(img.fwthr, p_fw) && up(img.area, p_area);
   ok = ok && up(img.zn, p_zn) && up(img.ze, p_ze) && up(img.cek, p_cek) && up(img.cnxc, p_cnxc) && up(img.cnyc, p_cnyc);
@@ -657,6 +690,7 @@ std::string Engine::init(std::vector<HostInstance>&& inst, int flux, int ws, int
   ok = ok && up(img.einst, p_einst) && up(img.enx, p_enx) && up(img.eny, p_eny) && up(img.etx, p_etx);
   ok = ok && up(img.ety, p_ety) && up(img.ezm, p_ezm) && up(img.elmin, p_elmin) && up(img.nz, p_nz);
   ok = ok && up(img.inst_cell_begin, p_icb) && up(img.inst_cfl, p_cfl) && up(img.inst_cor, p_cor);
+  ok = ok && up(img.srec, p_srec) && up(img.cslot, p_cslot) && up(img.erec, p_erec) && up(img.eidx, p_eidx);
   if (!ok) {
     *st = 6;
     return std::string("device allocation or upload failed: ") + cudaGetErrorString(cudaGetLastError());
@@ -667,6 +701,7 @@ std::string Engine::init(std::vector<HostInstance>&& inst, int flux, int ws, int
   M.eown = p_eown; M.enb = p_enb; M.eslotl = p_esl; M.eslotr = p_esr; M.einst = p_einst;
   M.enx = p_enx; M.eny = p_eny; M.etx = p_etx; M.ety = p_ety; M.ezm = p_ezm; M.elmin = p_elmin;
   M.nz = p_nz; M.inst_cell_begin = p_icb; M.inst_cfl = p_cfl; M.inst_cor = p_cor;
+  M.srec = p_srec; M.cslot = p_cslot; M.erec = p_erec; M.eidx = p_eidx;
 
   DevWork& Wk = work_;
   Wk.ew = dalloc<double>(3 * C); Wk.eu = dalloc<double>(3 * C); Wk.ev = dalloc<double>(3 * C);

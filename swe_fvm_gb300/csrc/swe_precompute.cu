@@ -27,6 +27,8 @@ void HostImage::resize(int C_, int E_, int N_, int I_) {
   cnxc.assign(3 * (size_t)C, 0); cnyc.assign(3 * (size_t)C, 0);
   dry.assign((size_t)C * kDryStride, 0); combo.assign((size_t)C * 8 * kComboStride, 0);
   pw1.assign((size_t)C * kPw1Stride, 0); pw2.assign(C, Pw2Rec{});
+  srec.assign(3 * (size_t)C, SlotRec{}); cslot.assign(3 * (size_t)C, int2{0, -1});
+  erec.assign(E, EdgeRec{}); eidx.assign(E, int4{0, -1, 0, -1});
   eown.assign(E, 0); enb.assign(E, -1); eslotl.assign(E, 0); eslotr.assign(E, -1); einst.assign(E, 0);
   enx.assign(E, 0); eny.assign(E, 0); etx.assign(E, 0); ety.assign(E, 0); ezm.assign(E, 0); elmin.assign(E, 0);
   nz.assign(N, 0);
@@ -186,6 +188,9 @@ void precompute_instance(const HostInstance& h, int inst, int64_t c0, int64_t e0
         // n(e, i) * c first), kept whole so the update multiplies once
         img.cnxc[k * Ct + gi] = nrm[0] * img.cek[k * Ct + gi];
         img.cnyc[k * Ct + gi] = nrm[1] * img.cek[k * Ct + gi];
+        img.srec[k * Ct + gi] = SlotRec{img.cek[k * Ct + gi], img.ze[k * Ct + gi], img.cnxc[k * Ct + gi],
+                                        img.cnyc[k * Ct + gi]};
+        img.cslot[k * Ct + gi] = int2{img.cedge[k * Ct + gi], img.cnbr[k * Ct + gi]};
       }
       // ---- dry cell: ReconstructDryCell + UpdateInterfaceValues
       // (src/MUSCLObject.cpp:31-36, include/MUSCLObject.h:26-33, src/Assigners.cpp:8-20)
@@ -225,7 +230,7 @@ void precompute_instance(const HostInstance& h, int inst, int64_t c0, int64_t e0
           double g0, g1;
           plane_gradient(pk[0][0], pk[0][1], pk[0][2], pk[1][0], pk[1][1], pk[1][2], pk[2][0], pk[2][1], pk[2][2],
                          &g0, &g1);
-          double* rec = img.combo.data() + ((size_t)gi * 8 + mask) * kComboStride;
+          double* rec = img.combo.data() + combo_off((int)Ct, (int)gi, mask);
           rec[0] = g0;
           rec[1] = g1;
           for (int k = 0; k < 3; ++k) {
@@ -325,6 +330,8 @@ void precompute_instance(const HostInstance& h, int inst, int64_t c0, int64_t e0
       } else {
         img.elmin[ge] = 0.;
       }
+      img.erec[ge] = EdgeRec{img.enx[ge], img.eny[ge], img.etx[ge], img.ety[ge], img.ezm[ge], img.elmin[ge]};
+      img.eidx[ge] = int4{img.eown[ge], img.enb[ge], img.eslotl[ge], img.eslotr[ge]};
     }
   };
 
