@@ -56,6 +56,49 @@ def workload():
     return mesh, prim, time.time() - t0
 
 
+def workload_config(mesh, world):
+    """The workload both arms run (the same dict in the GPU line and the
+    reference line)."""
+    return {"workload": "dam_break_1M", "cells": mesh.num_cells, "edges": mesh.num_edges, "nodes": mesh.num_nodes,
+            "flux": "HLLC+Einfeldt", "scheme": "SSPRK2", "cfl": CFL, "dt": "CFLdt() per step",
+            "l2": "working set > 1 GB, larger than the 129 MB L2; no flush", "parallelism": f"replicas x{world}"}
+
+
+def run_thacker(torch, stream, steps: int = 1000):
+    """Config: Thacker bowl on [-2,2]^2, 64 x 64 squares x 2 triangles (8192
+    cells), HLLC + Einfeldt, SSPRK2, CFL 0.4, 1000 steps with dt from the
+    device CFL reduction (graph-replayed), beside the single-thread CPU
+    restatement on the same run.  The GPU run's states equal the reference's
+    own solver bit for bit (tests/test_gpu_ref_golden.py)."""
+    from oracle.oracle import Oracle
+    from swe_fvm_gb300 import Fluxes, SpaceDisc, Wavespeeds, scenarios
+
+    m, prim = scenarios.thacker(64)
+    sd = SpaceDisc(Fluxes.HLLC(Wavespeeds.Einfeldt), m, prim, cfl=0.4)
+    sd.set_stream(stream.cuda_stream)
+    sd.ComputeInterfaceValues()
+    sd.ComputeFluxes()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    t_end = sd.run_cfl(1, steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    o = Oracle(m, prim)
+    o.compute_interface_values()
+    o.compute_fluxes()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        o.step("SSPRK2", 0.4 * o.min_len_to_wavespeed())
+    cpu_s = time.perf_counter() - t0
+    return {"metric": "cell-updates/s (Thacker 64x64x2, SSPRK2, CFL 0.4, 1000 steps)",
+            "value": m.num_cells * steps / (ms * 1e-3), "unit": "cell-updates/s", "ms_per_step": ms / steps,
+            "steps": steps, "simulated_time": t_end,
+            "note": "first 1000 steps from a fresh context, including the graph capture of the first replay",
+            "cpu_restatement_1_thread": m.num_cells * steps / cpu_s}
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
@@ -329,12 +372,10 @@ def run_gpu(args):
         "value": value, "unit": "cell-updates/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded jittered-lattice Delaunay mesh, Gaussian bumps, dam break)",
-        "config": {"workload": "dam_break_1M", "cells": C, "edges": mesh.num_edges, "nodes": mesh.num_nodes,
-                   "flux": "HLLC+Einfeldt", "scheme": "SSPRK2", "cfl": CFL, "dt": "CFLdt() per step, on device",
-                   "l2": "working set > 1 GB, larger than the 129 MB L2; no flush",
-                   "parallelism": f"replicas x{world}", "mesh_gen_s": round(t_gen, 1),
-                   "tuning": sd.tuning()},
+        "config": workload_config(mesh, world),
+        "tuning": sd.tuning(), "mesh_gen_s": round(t_gen, 1),
         "e2e": e2e, "gpu_launches": launches, "roofline": roof, "clocks": clk.summary(), "hll": hll,
+        "thacker_8192": run_thacker(torch, stream),
     }
     if ENSEMBLE_INSTANCES > 0 and not args.no_ensemble:
         out["batched"] = run_ensemble(torch, stream)
@@ -578,9 +619,10 @@ TRAFFIC_PER_STEP = {708: 1.753e9}
 
 
 def run_reference(args):
-    """CPU restatement of the reference solver on all host threads (the
-    reference cannot be built here: Eigen is fetched from the network at
-    configure time)."""
+    """The reference's CPU step on all host threads.  The reference's own
+    sources cannot travel to the GPU machine, so this times the C restatement,
+    which equals the reference built from its sources bit for bit (Q1/Q20
+    edits, tests/test_ref_pin.py), in jacobi loop order on OpenMP threads."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
@@ -588,6 +630,7 @@ def run_reference(args):
 
     mesh, prim, _ = workload()
     C = mesh.num_cells
+    world = int(os.environ.get("WORLD_SIZE", "1"))
     o = Oracle(mesh, prim)
     # every host thread this process may use: the restatement's jacobi-order
     # loops under OpenMP (results equal the single-thread ones bit for bit)
@@ -598,7 +641,7 @@ def run_reference(args):
     o.set_threads(threads)
     o.compute_interface_values()
     o.compute_fluxes()
-    for _ in range(min(args.warmup, 1)):
+    for _ in range(args.warmup):
         o.step("SSPRK2", CFL * o.min_len_to_wavespeed())
     budget = 120.0
     done, t = 0, 0.0
@@ -610,13 +653,15 @@ def run_reference(args):
         if t > budget:
             break
     value = C * done / t
-    sample = f"{done} of {args.steps} SSPRK2 steps of the full {C}-cell mesh, {threads} threads ({t:.1f} s)"
+    sample = (f"{done} of {args.steps} SSPRK2 steps of the full {C}-cell mesh, {threads} threads ({t:.1f} s); "
+              "the C restatement in jacobi loop order (OpenMP), equal bit for bit to the reference's own solver "
+              "built from its sources (tests/test_ref_pin.py); the reference's literal loop order runs on one "
+              "thread only")
     out = {"impl": "reference", "metric": "cell-updates/s (plain FP64 SSPRK2 step, 1M-triangle unstructured mesh)",
-           "value": value, "unit": "cell-updates/s", "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
+           "value": value, "unit": "cell-updates/s", "n_gpus": world,
            "steps": done, "warmup": args.warmup, "ms_per_step": 1e3 * t / done, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-           "config": {"workload": "dam_break_1M", "cells": C, "flux": "HLLC+Einfeldt", "scheme": "SSPRK2",
-                      "cfl": CFL},
+           "config": workload_config(mesh, world),
            "cpu_baseline": {"value": value, "unit": "cell-updates/s", "cores": threads, "kind": "port",
                             "sample": sample},
            "e2e": {"value": value, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
