@@ -298,6 +298,35 @@ swe_status swe_adjoint_forward(swe_ctx* ctx, int32_t scheme, int64_t n_steps, in
 swe_status swe_adjoint_backward(swe_ctx* ctx, const double* trace_grads, double* grad_prim0, double* grad_bathymetry);
 /* The n_steps dts recorded by the last swe_adjoint_forward. */
 swe_status swe_adjoint_dts(swe_ctx* ctx, double* dts_out);
+/* swe_adjoint_forward / swe_adjoint_backward with every array in device memory
+ * (gauge_cells stays on the host): traces_out, trace_grads, grad_prim0 (3 x C
+ * interleaved, the caller's cell order) and grad_bathymetry (N, the caller's
+ * node order) are device pointers; the work runs on the context's stream. */
+swe_status swe_adjoint_forward_device(swe_ctx* ctx, int32_t scheme, int64_t n_steps, int64_t checkpoint_every,
+                                      int32_t n_gauges, const int64_t* gauge_cells, int64_t obs_every,
+                                      double* traces_out);
+swe_status swe_adjoint_backward_device(swe_ctx* ctx, const double* trace_grads, double* grad_prim0,
+                                       double* grad_bathymetry);
+/* A forward run with prescribed dts and no tape: n_steps steps of `scheme`,
+ * step n with dt = dts[n], and w at the gauge cells after every obs_every-th
+ * step into traces_out (host, n_steps / obs_every rows of n_gauges).  With the
+ * dts a taped run recorded (swe_adjoint_dts) it repeats that run's steps for a
+ * perturbed initial state or bed: what finite-difference checks of the
+ * adjoint need.  No reference counterpart. */
+swe_status swe_run_traces(swe_ctx* ctx, int32_t scheme, int64_t n_steps, const double* dts, int32_t n_gauges,
+                          const int64_t* gauge_cells, int64_t obs_every, double* traces_out);
+/* Replaces the node bathymetry (N values, the caller's node order, host) of a
+ * context: every mesh record that depends on it is recomputed with the
+ * reference's operation order and re-uploaded in place (device order, tuning
+ * and captured graphs kept); the state is kept and the adjoint's tape is
+ * dropped.  The reference's geometry is a caller array (include/Bathymetry.h:
+ * 42-43), so writing its z row and stepping again is the reference-side
+ * equivalent.  Call swe_prime afterwards for a CFLdt() of the new bed. */
+swe_status swe_set_bathymetry(swe_ctx* ctx, const double* z);
+/* Recomputes the flux pass of the current state (SpaceDisc::
+ * ComputeInterfaceValues + ComputeFluxes, src/SpaceDisc.cpp:33-74) so that
+ * CFLdt() and the next CFL step follow from it, as after swe_create. */
+swe_status swe_prime(swe_ctx* ctx);
 
 /* ---------------------------------------------------------------- batched */
 /* Many independent instances (each its own mesh, state, parameters and CFL
@@ -353,6 +382,23 @@ swe_status swe_batch_adjoint_forward(swe_batch* b, int32_t scheme, int64_t n_ste
 swe_status swe_batch_adjoint_backward(swe_batch* b, const double* trace_grads, double* grad_prim0,
                                       double* grad_bathymetry);
 swe_status swe_batch_adjoint_dts(swe_batch* b, double* dts_out);
+/* Device-memory forms of the batch adjoint, as for a single context. */
+swe_status swe_batch_adjoint_forward_device(swe_batch* b, int32_t scheme, int64_t n_steps, int64_t checkpoint_every,
+                                            int32_t n_gauges, const int64_t* gauge_cells, int64_t obs_every,
+                                            double* traces_out);
+swe_status swe_batch_adjoint_backward_device(swe_batch* b, const double* trace_grads, double* grad_prim0,
+                                             double* grad_bathymetry);
+/* swe_run_traces for a batch: dts is n_steps x n_instances (step-major, each
+ * instance its own dt); gauges numbered over the concatenation. */
+swe_status swe_batch_run_traces(swe_batch* b, int32_t scheme, int64_t n_steps, const double* dts, int32_t n_gauges,
+                                const int64_t* gauge_cells, int64_t obs_every, double* traces_out);
+/* swe_set_bathymetry for a batch: z[q] (N_q values, host) for every instance
+ * whose bed changes, NULL for the others; one recompute and re-upload. */
+swe_status swe_batch_set_bathymetry(swe_batch* b, const double* const* z);
+/* swe_prime for every instance of a batch. */
+swe_status swe_batch_prime(swe_batch* b);
+/* swe_set_prim_device for instance q of a batch (3 x C_q interleaved, device). */
+swe_status swe_batch_set_prim_device(swe_batch* b, int32_t q, const double* prim_in);
 
 #ifdef __cplusplus
 }

@@ -36,7 +36,10 @@ EXPORTS = [
     "swe_integrals", "swe_batch_integrals", "swe_get_tuning", "swe_batch_get_tuning", "swe_layout_plan",
     "swe_set_scheme", "swe_batch_set_scheme", "swe_get_time", "swe_set_time", "swe_batch_set_time",
     "swe_batch_set_prim", "swe_set_min_len_to_wavespeed", "swe_batch_min_len_to_wavespeed",
-    "swe_batch_set_min_len_to_wavespeed",
+    "swe_batch_set_min_len_to_wavespeed", "swe_adjoint_forward_device", "swe_adjoint_backward_device",
+    "swe_run_traces", "swe_set_bathymetry", "swe_prime", "swe_batch_adjoint_forward_device",
+    "swe_batch_adjoint_backward_device", "swe_batch_run_traces", "swe_batch_set_bathymetry", "swe_batch_prime",
+    "swe_batch_set_prim_device",
 ]
 
 
@@ -154,6 +157,17 @@ def load(build_if_needed: bool = True):
         "swe_set_min_len_to_wavespeed": [vp, d],
         "swe_batch_min_len_to_wavespeed": [vp, i32, P(d)],
         "swe_batch_set_min_len_to_wavespeed": [vp, i32, d],
+        "swe_adjoint_forward_device": [vp, i32, i64, i64, i32, vp, i64, vp],
+        "swe_adjoint_backward_device": [vp, vp, vp, vp],
+        "swe_run_traces": [vp, i32, i64, vp, i32, vp, i64, vp],
+        "swe_set_bathymetry": [vp, vp],
+        "swe_prime": [vp],
+        "swe_batch_adjoint_forward_device": [vp, i32, i64, i64, i32, vp, i64, vp],
+        "swe_batch_adjoint_backward_device": [vp, vp, vp, vp],
+        "swe_batch_run_traces": [vp, i32, i64, vp, i32, vp, i64, vp],
+        "swe_batch_set_bathymetry": [vp, vp],
+        "swe_batch_prime": [vp],
+        "swe_batch_set_prim_device": [vp, i32, vp],
     }
     for name, args in sig.items():
         f = getattr(L, name)

@@ -764,6 +764,101 @@ swe_status swe_adjoint_backward(swe_ctx* ctx, const double* trace_grads, double*
   SWE_GUARD_END(&ctx->err)
 }
 
+// gauges in the caller's numbering -> device positions; "" or why not
+std::string map_gauges(const Engine& g, int32_t n_gauges, const int64_t* gauge_cells, std::vector<int>* out) {
+  out->assign(n_gauges > 0 ? n_gauges : 0, 0);
+  for (int q = 0; q < n_gauges; ++q) {
+    if (gauge_cells[q] < 0 || gauge_cells[q] >= g.C()) return "gauge cell out of range";
+    (*out)[q] = (int)device_cell(g, gauge_cells[q]);
+  }
+  return "";
+}
+
+swe_status run_traces_common(Engine& eng, std::string* err, int32_t scheme, int64_t n_steps, const double* dts,
+                             int32_t n_gauges, const int64_t* gauge_cells, int64_t obs_every, double* traces_out) {
+  if (!eng.has_scheme(scheme) || n_steps <= 0 || n_gauges < 0 || obs_every <= 0 || !dts)
+    return fail(err, SWE_ERR_INVALID_ARGUMENT, "bad scheme, step counts, gauge count or dts");
+  if (n_gauges > 0 && (!gauge_cells || !traces_out))
+    return fail(err, SWE_ERR_INVALID_ARGUMENT, "gauge_cells and traces_out are required");
+  for (int64_t k = 0; k < n_steps * (int64_t)eng.I(); ++k)
+    if (!(dts[k] > 0.) || !std::isfinite(dts[k]))
+      return fail(err, SWE_ERR_INVALID_ARGUMENT, "every dt must be positive and finite");
+  std::vector<int> g;
+  std::string e = map_gauges(eng, n_gauges, gauge_cells, &g);
+  if (!e.empty()) return fail(err, SWE_ERR_INVALID_ARGUMENT, e);
+  e = eng.run_traces(scheme, n_steps, dts, g.data(), n_gauges, obs_every, traces_out);
+  if (!e.empty()) return fail(err, SWE_ERR_CUDA, e);
+  return SWE_OK;
+}
+
+swe_status adjoint_forward_device_common(Engine& eng, std::string* err, int32_t scheme, int64_t n_steps,
+                                         int64_t checkpoint_every, int32_t n_gauges, const int64_t* gauge_cells,
+                                         int64_t obs_every, double* traces_out) {
+  if (!eng.has_scheme(scheme) || n_steps <= 0 || checkpoint_every <= 0 || n_gauges < 0 || obs_every <= 0)
+    return fail(err, SWE_ERR_INVALID_ARGUMENT, "bad scheme, step counts or gauge count");
+  if (n_gauges > 0 && (!gauge_cells || !traces_out))
+    return fail(err, SWE_ERR_INVALID_ARGUMENT, "gauge_cells and traces_out are required");
+  std::vector<int> g;
+  std::string e = map_gauges(eng, n_gauges, gauge_cells, &g);
+  if (!e.empty()) return fail(err, SWE_ERR_INVALID_ARGUMENT, e);
+  e = eng.adjoint_forward(scheme, n_steps, checkpoint_every, g.data(), n_gauges, obs_every, traces_out, true);
+  if (!e.empty()) return fail(err, SWE_ERR_CUDA, e);
+  return SWE_OK;
+}
+
+swe_status set_bathymetry_common(Engine& eng, std::string* err, const std::vector<const double*>& z) {
+  std::string e = eng.set_bathymetry(z);
+  if (e.empty()) return SWE_OK;
+  if (e.find("non-finite") != std::string::npos) return fail(err, SWE_ERR_NONFINITE, e);
+  return fail(err, SWE_ERR_CUDA, e);
+}
+
+swe_status swe_run_traces(swe_ctx* ctx, int32_t scheme, int64_t n_steps, const double* dts, int32_t n_gauges,
+                          const int64_t* gauge_cells, int64_t obs_every, double* traces_out) {
+  Trace trace("swe_run_traces");
+  if (!ctx) return SWE_ERR_INVALID_ARGUMENT;
+  SWE_GUARD_BEGIN
+  return run_traces_common(ctx->eng, &ctx->err, scheme, n_steps, dts, n_gauges, gauge_cells, obs_every, traces_out);
+  SWE_GUARD_END(&ctx->err)
+}
+
+swe_status swe_set_bathymetry(swe_ctx* ctx, const double* z) {
+  Trace trace("swe_set_bathymetry");
+  if (!ctx || !z) return SWE_ERR_INVALID_ARGUMENT;
+  SWE_GUARD_BEGIN
+  return set_bathymetry_common(ctx->eng, &ctx->err, std::vector<const double*>{z});
+  SWE_GUARD_END(&ctx->err)
+}
+
+swe_status swe_prime(swe_ctx* ctx) {
+  if (!ctx) return SWE_ERR_INVALID_ARGUMENT;
+  SWE_GUARD_BEGIN
+  return prime(ctx->eng, &ctx->err);
+  SWE_GUARD_END(&ctx->err)
+}
+
+swe_status swe_adjoint_forward_device(swe_ctx* ctx, int32_t scheme, int64_t n_steps, int64_t checkpoint_every,
+                                      int32_t n_gauges, const int64_t* gauge_cells, int64_t obs_every,
+                                      double* traces_out) {
+  Trace trace("swe_adjoint_forward_device");
+  if (!ctx) return SWE_ERR_INVALID_ARGUMENT;
+  SWE_GUARD_BEGIN
+  return adjoint_forward_device_common(ctx->eng, &ctx->err, scheme, n_steps, checkpoint_every, n_gauges, gauge_cells,
+                                       obs_every, traces_out);
+  SWE_GUARD_END(&ctx->err)
+}
+
+swe_status swe_adjoint_backward_device(swe_ctx* ctx, const double* trace_grads, double* grad_prim0,
+                                       double* grad_bathymetry) {
+  Trace trace("swe_adjoint_backward_device");
+  if (!ctx || !grad_prim0 || !grad_bathymetry) return SWE_ERR_INVALID_ARGUMENT;
+  SWE_GUARD_BEGIN
+  std::string e = ctx->eng.adjoint_backward(trace_grads, grad_prim0, grad_bathymetry, true);
+  if (!e.empty()) return fail(&ctx->err, SWE_ERR_INVALID_ARGUMENT, e);
+  return SWE_OK;
+  SWE_GUARD_END(&ctx->err)
+}
+
 swe_status swe_adjoint_dts(swe_ctx* ctx, double* dts_out) {
   if (!ctx || !dts_out) return SWE_ERR_INVALID_ARGUMENT;
   std::string e = ctx->eng.adjoint_dts(dts_out);
@@ -979,6 +1074,64 @@ swe_status swe_batch_adjoint_backward(swe_batch* b, const double* trace_grads, d
   if (!b || !grad_prim0 || !grad_bathymetry) return SWE_ERR_INVALID_ARGUMENT;
   SWE_GUARD_BEGIN
   std::string e = adjoint_backward_caller(b->eng, trace_grads, grad_prim0, grad_bathymetry);
+  if (!e.empty()) return fail(&b->err, SWE_ERR_INVALID_ARGUMENT, e);
+  return SWE_OK;
+  SWE_GUARD_END(&b->err)
+}
+
+swe_status swe_batch_run_traces(swe_batch* b, int32_t scheme, int64_t n_steps, const double* dts, int32_t n_gauges,
+                                const int64_t* gauge_cells, int64_t obs_every, double* traces_out) {
+  Trace trace("swe_batch_run_traces");
+  if (!b) return SWE_ERR_INVALID_ARGUMENT;
+  SWE_GUARD_BEGIN
+  return run_traces_common(b->eng, &b->err, scheme, n_steps, dts, n_gauges, gauge_cells, obs_every, traces_out);
+  SWE_GUARD_END(&b->err)
+}
+
+swe_status swe_batch_set_bathymetry(swe_batch* b, const double* const* z) {
+  Trace trace("swe_batch_set_bathymetry");
+  if (!b || !z) return SWE_ERR_INVALID_ARGUMENT;
+  SWE_GUARD_BEGIN
+  return set_bathymetry_common(b->eng, &b->err, std::vector<const double*>(z, z + b->eng.I()));
+  SWE_GUARD_END(&b->err)
+}
+
+swe_status swe_batch_prime(swe_batch* b) {
+  if (!b) return SWE_ERR_INVALID_ARGUMENT;
+  SWE_GUARD_BEGIN
+  return prime(b->eng, &b->err);
+  SWE_GUARD_END(&b->err)
+}
+
+swe_status swe_batch_set_prim_device(swe_batch* b, int32_t q, const double* in) {
+  if (!b || !in || q < 0 || q >= b->eng.I()) return SWE_ERR_INVALID_ARGUMENT;
+  Engine& g = b->eng;
+  const int64_t c0 = g.cell_off[q], n = g.cell_off[q + 1] - c0;
+  k_unpack<<<(int)((n + 255) / 256), 256, 0, g.stream()>>>(in, g.state(0, 0) + c0, g.state(0, 1) + c0,
+                                                            g.state(0, 2) + c0, (int)n, nullptr,
+                                                            g.d_cell_from ? g.d_cell_from + c0 : nullptr);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(&b->err, e, "swe_batch_set_prim_device");
+  return SWE_OK;
+}
+
+swe_status swe_batch_adjoint_forward_device(swe_batch* b, int32_t scheme, int64_t n_steps, int64_t checkpoint_every,
+                                            int32_t n_gauges, const int64_t* gauge_cells, int64_t obs_every,
+                                            double* traces_out) {
+  Trace trace("swe_batch_adjoint_forward_device");
+  if (!b) return SWE_ERR_INVALID_ARGUMENT;
+  SWE_GUARD_BEGIN
+  return adjoint_forward_device_common(b->eng, &b->err, scheme, n_steps, checkpoint_every, n_gauges, gauge_cells,
+                                       obs_every, traces_out);
+  SWE_GUARD_END(&b->err)
+}
+
+swe_status swe_batch_adjoint_backward_device(swe_batch* b, const double* trace_grads, double* grad_prim0,
+                                             double* grad_bathymetry) {
+  Trace trace("swe_batch_adjoint_backward_device");
+  if (!b || !grad_prim0 || !grad_bathymetry) return SWE_ERR_INVALID_ARGUMENT;
+  SWE_GUARD_BEGIN
+  std::string e = b->eng.adjoint_backward(trace_grads, grad_prim0, grad_bathymetry, true);
   if (!e.empty()) return fail(&b->err, SWE_ERR_INVALID_ARGUMENT, e);
   return SWE_OK;
   SWE_GUARD_END(&b->err)

@@ -987,7 +987,7 @@ std::string Engine::adjoint_init() {
 }
 
 std::string Engine::adjoint_forward(int scheme, int64_t n_steps, int64_t ckpt, const int* gauges, int n_gauges,
-                                    int64_t obs, double* traces_host) {
+                                    int64_t obs, double* traces_host, bool traces_device) {
   std::string err = adjoint_init();
   if (!err.empty()) return err;
   AdjointState& a = *adj_;
@@ -1031,10 +1031,72 @@ std::string Engine::adjoint_forward(int scheme, int64_t n_steps, int64_t ckpt, c
     }
   }
   if (traces_host && n_obs * n_gauges > 0)
-    cudaMemcpyAsync(traces_host, a.d_traces, n_obs * n_gauges * sizeof(double), cudaMemcpyDeviceToHost, stream_);
+    cudaMemcpyAsync(traces_host, a.d_traces, n_obs * n_gauges * sizeof(double),
+                    traces_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, stream_);
   cudaError_t e = cudaStreamSynchronize(stream_);
   if (e != cudaSuccess) return std::string("taped forward run: ") + cudaGetErrorString(e);
   a.taped = true;
+  return "";
+}
+
+std::string Engine::run_traces(int scheme, int64_t n_steps, const double* dts_host, const int* gauges, int n_gauges,
+                               int64_t obs, double* traces_host) {
+  const int64_t NI = I();
+  const int64_t n_obs = obs > 0 ? n_steps / obs : 0;
+  double *d_dts = nullptr, *d_tr = nullptr;
+  int* d_g = nullptr;
+  std::string err;
+  auto release = [&] {
+    if (d_dts) cudaFree(d_dts);
+    if (d_tr) cudaFree(d_tr);
+    if (d_g) cudaFree(d_g);
+  };
+  if (cudaMalloc(&d_dts, (n_steps ? n_steps : 1) * NI * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&d_tr, (n_obs * n_gauges ? n_obs * n_gauges : 1) * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&d_g, (n_gauges ? n_gauges : 1) * sizeof(int)) != cudaSuccess) {
+    release();
+    return "allocation failed";
+  }
+  cudaError_t e = cudaMemcpyAsync(d_dts, dts_host, n_steps * NI * sizeof(double), cudaMemcpyHostToDevice, stream_);
+  if (e == cudaSuccess && n_gauges)
+    e = cudaMemcpyAsync(d_g, gauges, n_gauges * sizeof(int), cudaMemcpyHostToDevice, stream_);
+  for (int64_t n = 0; n < n_steps && e == cudaSuccess; ++n) {
+    // the step's dt per instance, then one replay of the fixed-dt step graph
+    e = cudaMemcpyAsync(d_fixed_dt, d_dts + n * NI, NI * sizeof(double), cudaMemcpyDeviceToDevice, stream_);
+    if (e == cudaSuccess) e = run_graph(scheme, 2, 1);
+    if (e == cudaSuccess && obs > 0 && (n + 1) % obs == 0 && n_gauges > 0) {
+      const int64_t j = (n + 1) / obs - 1;
+      k_gather_gauges<<<(n_gauges + 255) / 256, 256, 0, stream_>>>(state(0, 0), d_g, n_gauges, d_tr + j * n_gauges);
+      ++launches_;
+      e = cudaGetLastError();
+    }
+  }
+  if (e == cudaSuccess && traces_host && n_obs * n_gauges > 0)
+    e = cudaMemcpyAsync(traces_host, d_tr, n_obs * n_gauges * sizeof(double), cudaMemcpyDeviceToHost, stream_);
+  cudaError_t e2 = cudaStreamSynchronize(stream_);
+  if (e == cudaSuccess) e = e2;
+  if (e != cudaSuccess) err = std::string("trace run: ") + cudaGetErrorString(e);
+  release();
+  return err;
+}
+
+std::string Engine::caller_maps() {
+  if (d_cell_caller && d_node_caller) return "";
+  std::vector<int> cm((size_t)mesh_.C), nm((size_t)mesh_.N);
+  for (size_t q = 0; q < host.size(); ++q) {
+    const Layout* L = q < layouts.size() ? &layouts[q] : nullptr;
+    const bool id = !L || L->identity();
+    for (int64_t j = 0; j < cell_off[q + 1] - cell_off[q]; ++j)
+      cm[cell_off[q] + j] = (int)(cell_off[q] + (id ? j : L->cell_from[j]));
+    for (int64_t j = 0; j < node_off[q + 1] - node_off[q]; ++j)
+      nm[node_off[q] + j] = (int)(node_off[q] + (id ? j : L->node_from[j]));
+  }
+  d_cell_caller = dalloc<int>(cm.size());
+  d_node_caller = dalloc<int>(nm.size());
+  if (!d_cell_caller || !d_node_caller) return "device allocation failed";
+  if (cudaMemcpy(d_cell_caller, cm.data(), cm.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(d_node_caller, nm.data(), nm.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess)
+    return std::string("uploading the caller order: ") + cudaGetErrorString(cudaGetLastError());
   return "";
 }
 
@@ -1053,8 +1115,20 @@ __global__ void k_interleave(const double* W, int C, double* out) {
   }
 }
 
-std::string Engine::adjoint_backward(const double* trace_grads_host, double* grad_prim_host, double* grad_z_host) {
+// out[w * map[i] + c] = in[w * i + c]: device rows to the caller's order
+__global__ void k_rows_to_caller(const double* in, const int* map, int n, int w, double* out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n)
+    for (int c = 0; c < w; ++c) out[(size_t)w * map[i] + c] = in[(size_t)w * i + c];
+}
+
+std::string Engine::adjoint_backward(const double* trace_grads_host, double* grad_prim_host, double* grad_z_host,
+                                     bool device) {
   if (!adj_ || !adj_->taped) return "no taped forward run to differentiate";
+  if (device) {
+    std::string e = caller_maps();
+    if (!e.empty()) return e;
+  }
   AdjointState& a = *adj_;
   AdjWork& w = a.aw;
   const int64_t C = mesh_.C, N = mesh_.N;
@@ -1065,7 +1139,8 @@ std::string Engine::adjoint_backward(const double* trace_grads_host, double* gra
   if (cudaMalloc(&d_tg, (n_obs * a.n_gauges ? n_obs * a.n_gauges : 1) * sizeof(double)) != cudaSuccess)
     return "allocation failed";
   if (n_obs * a.n_gauges)
-    cudaMemcpy(d_tg, trace_grads_host, n_obs * a.n_gauges * sizeof(double), cudaMemcpyHostToDevice);
+    cudaMemcpy(d_tg, trace_grads_host, n_obs * a.n_gauges * sizeof(double),
+               device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice);
   // stage-input store of one segment: [K][ns] states of 3C, plus the segment end
   const int64_t K = a.ckpt;
   std::vector<double*> store((size_t)K * ns + 1, nullptr);
@@ -1259,8 +1334,14 @@ std::string Engine::adjoint_backward(const double* trace_grads_host, double* gra
   if (err.empty()) {
     double* d_out = store[0];
     k_interleave<<<gc, b, 0, stream_>>>(lam_step, (int)C, d_out);
-    cudaMemcpyAsync(grad_prim_host, d_out, 3 * C * sizeof(double), cudaMemcpyDeviceToHost, stream_);
-    cudaMemcpyAsync(grad_z_host, w.lz, N * sizeof(double), cudaMemcpyDeviceToHost, stream_);
+    if (device) {
+      k_rows_to_caller<<<gc, b, 0, stream_>>>(d_out, d_cell_caller, (int)C, 3, grad_prim_host);
+      k_rows_to_caller<<<(int)((N + b - 1) / b), b, 0, stream_>>>(w.lz, d_node_caller, (int)N, 1, grad_z_host);
+      launches_ += 2;
+    } else {
+      cudaMemcpyAsync(grad_prim_host, d_out, 3 * C * sizeof(double), cudaMemcpyDeviceToHost, stream_);
+      cudaMemcpyAsync(grad_z_host, w.lz, N * sizeof(double), cudaMemcpyDeviceToHost, stream_);
+    }
     cudaError_t e = cudaStreamSynchronize(stream_);
     if (e != cudaSuccess) err = std::string("adjoint: ") + cudaGetErrorString(e);
   }

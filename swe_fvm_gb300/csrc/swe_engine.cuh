@@ -228,6 +228,12 @@ class Engine {
   int* d_cell_from = nullptr;
   int* d_cell_to = nullptr;
   std::string set_layouts(std::vector<Layout>&& lay);
+  // Replaces the node bathymetry of the instances whose pointer is not null
+  // (each in the caller's node order, N_q values), recomputes every mesh record
+  // with the same device order and re-uploads them into the same buffers (the
+  // captured step graphs stay valid); drops the adjoint's tape.  The state is
+  // kept; the caller re-primes the flux pass.
+  std::string set_bathymetry(const std::vector<const double*>& z);
   // Mean ms of one graph-replayed step of `scheme` (CFL dt) over n steps after
   // one warm-up replay, run from the current state, which is then restored
   // with the accumulated time, the step dt and the error word (the caller
@@ -275,12 +281,22 @@ class Engine {
   // state, checkpoint every ckpt steps, w at the gauge cells every obs steps
   // into traces_host (n_steps / obs rows).  Returns "" or an error message.
   std::string adjoint_init();
+  // traces_device: traces_host is a device pointer (the traces are copied on
+  // the device).
   std::string adjoint_forward(int scheme, int64_t n_steps, int64_t ckpt, const int* gauges, int n_gauges,
-                              int64_t obs, double* traces_host);
+                              int64_t obs, double* traces_host, bool traces_device = false);
+  // n_steps steps of `scheme` with the given dts (n_steps x I, step-major),
+  // w at the gauge cells after every obs-th step into traces (n_steps / obs
+  // rows); no tape.  Returns "" or an error message.
+  std::string run_traces(int scheme, int64_t n_steps, const double* dts_host, const int* gauges, int n_gauges,
+                         int64_t obs, double* traces_host);
   // Reverse of the taped run: trace_grads (n_obs x n_gauges) are the adjoints
   // of the traces; returns the gradient with respect to the initial primitive
   // state (3 x C interleaved) and the node bathymetry (N).
-  std::string adjoint_backward(const double* trace_grads_host, double* grad_prim_host, double* grad_z_host);
+  // device: every pointer is device memory and the gradients are written in
+  // the caller's cell and node order.
+  std::string adjoint_backward(const double* trace_grads_host, double* grad_prim_host, double* grad_z_host,
+                               bool device = false);
   std::string adjoint_dts(double* out_host);
 
   int C() const { return mesh_.C; }
@@ -297,6 +313,11 @@ class Engine {
   std::vector<int64_t> cell_off, edge_off, node_off;
   // Host copies of the per-instance topology needed by the layout getters.
   std::vector<HostInstance> host;
+  // global device cell / node position -> global caller index, built on first
+  // use by the device-memory adjoint outputs
+  int* d_cell_caller = nullptr;
+  int* d_node_caller = nullptr;
+  std::string caller_maps();
   double* d_io = nullptr;        // [3C] staging buffer for the interleaved 3 x C field
   unsigned* d_ioflag = nullptr;  // non-finite flag of the last upload
   double* d_fixed_dt = nullptr;  // [I] device dt of fixed-step runs
@@ -339,6 +360,7 @@ class Engine {
   cudaGraphExec_t graphs_[4][3] = {};  // [scheme id][latch mode]
   Scheme custom_{};
   AdjointState* adj_ = nullptr;
+  std::vector<std::pair<void*, size_t>> mesh_arrays_;  // device mesh records in upload order
 };
 
 // Precompute (swe_precompute.cu): fills the host images of DevMesh arrays for

@@ -662,12 +662,16 @@ std::string Engine::init(std::vector<HostInstance>&& inst, int flux, int ws, int
   img.resize((int)C, (int)E, (int)N, I);
   for (int q = 0; q < I; ++q) precompute_instance(inst[q], q, cell_off[q], edge_off[q], node_off[q], img);
 
+  // every mesh array is recorded (device pointer, bytes) in upload order, so
+  // that set_bathymetry can refill the same buffers
+  mesh_arrays_.clear();
   auto up = [&](auto& vec, auto*& dst) -> bool {
     using T = typename std::remove_reference<decltype(vec)>::type::value_type;
     T* d = dalloc<T>(vec.size());
     if (!d) return false;
     if (cudaMemcpy(d, vec.data(), vec.size() * sizeof(T), cudaMemcpyHostToDevice) != cudaSuccess) return false;
     dst = d;
+    mesh_arrays_.push_back({(void*)d, vec.size() * sizeof(T)});
     return true;
   };
   DevMesh& M = mesh_;
@@ -1096,6 +1100,58 @@ std::string Engine::set_layouts(std::vector<Layout>&& lay) {
       cudaMemcpy(d_cell_to, to.data(), to.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess)
     return std::string("uploading the cell layout: ") + cudaGetErrorString(cudaGetLastError());
   return "";
+}
+
+std::string Engine::set_bathymetry(const std::vector<const double*>& z) {
+  if (z.size() != host.size()) return "one bathymetry pointer per instance is required";
+  for (size_t q = 0; q < host.size(); ++q) {
+    if (!z[q]) continue;
+    const HostInstance& h = host[q];
+    const Layout* L = q < layouts.size() ? &layouts[q] : nullptr;
+    for (int64_t p = 0; p < h.N; ++p)
+      if (!std::isfinite(z[q][(L && !L->identity()) ? L->node_from[p] : p])) return "bathymetry has a non-finite value";
+  }
+  for (size_t q = 0; q < host.size(); ++q) {
+    if (!z[q]) continue;
+    HostInstance& h = host[q];
+    const Layout* L = q < layouts.size() ? &layouts[q] : nullptr;
+    for (int64_t p = 0; p < h.N; ++p) h.geom[3 * p + 2] = z[q][(L && !L->identity()) ? L->node_from[p] : p];
+  }
+  const int I = (int)host.size();
+  HostImage img;
+  img.resize(mesh_.C, mesh_.E, mesh_.N, I);
+  for (int q = 0; q < I; ++q) precompute_instance(host[q], q, cell_off[q], edge_off[q], node_off[q], img);
+  // the same arrays, in the order init uploaded them
+  size_t k = 0;
+  bool ok = true;
+  auto refill = [&](auto& vec) {
+    using T = typename std::remove_reference<decltype(vec)>::type::value_type;
+    if (!ok || k >= mesh_arrays_.size() || mesh_arrays_[k].second != vec.size() * sizeof(T)) {
+      ok = false;
+      return;
+    }
+    ok = cudaMemcpyAsync(mesh_arrays_[k].first, vec.data(), vec.size() * sizeof(T), cudaMemcpyHostToDevice,
+                         stream_) == cudaSuccess;
+    ++k;
+  };
+  refill(img.cnode); refill(img.cnbr); refill(img.cedge); refill(img.cinst);
+  refill(img.cown); refill(img.bc); refill(img.fwthr); refill(img.area);
+  refill(img.zn); refill(img.ze); refill(img.cek); refill(img.cnxc); refill(img.cnyc);
+  refill(img.dry); refill(img.combo); refill(img.pw1); refill(img.pw2);
+  refill(img.eown); refill(img.enb); refill(img.eslotl); refill(img.eslotr);
+  refill(img.einst); refill(img.enx); refill(img.eny); refill(img.etx);
+  refill(img.ety); refill(img.ezm); refill(img.elmin); refill(img.nz);
+  refill(img.inst_cell_begin); refill(img.inst_cfl); refill(img.inst_cor);
+  refill(img.srec); refill(img.cslot); refill(img.erec); refill(img.eidx);
+  if (!ok || k != mesh_arrays_.size()) return "re-uploading the mesh records failed";
+  // the host image must outlive the asynchronous copies
+  cudaError_t e = cudaStreamSynchronize(stream_);
+  // the adjoint's tape and tables belong to the old bed
+  if (adj_) {
+    adjoint_state_delete(adj_);
+    adj_ = nullptr;
+  }
+  return e == cudaSuccess ? "" : std::string("re-uploading the mesh records: ") + cudaGetErrorString(e);
 }
 
 cudaError_t Engine::update_only(const Stage& st, const double* const* in, const double* const* u0,

@@ -350,6 +350,26 @@ class SpaceDisc:
     def set_stream(self, stream_ptr: int) -> None:
         self._check(_lib.load().swe_set_stream(self.ctx, ctypes.c_void_p(stream_ptr)))
 
+    def set_bathymetry(self, z) -> None:
+        """Replaces the node bathymetry (N values, the caller's node order):
+        the mesh records are recomputed and re-uploaded in place."""
+        a = np.ascontiguousarray(z, dtype=np.float64).reshape(self.num_nodes)
+        self._check(_lib.load().swe_set_bathymetry(self.ctx, a.ctypes.data))
+
+    def prime(self) -> None:
+        """The flux pass of the current state (CFLdt() then follows from it)."""
+        self._check(_lib.load().swe_prime(self.ctx))
+
+    def run_traces(self, scheme: int, dts, gauges, obs_every: int) -> np.ndarray:
+        """len(dts) steps with the given dts; w at the gauge cells after every
+        obs_every-th step, (len(dts) // obs_every, len(gauges))."""
+        d = np.ascontiguousarray(dts, dtype=np.float64)
+        g = np.ascontiguousarray(gauges, dtype=np.int64)
+        out = np.zeros((len(d) // obs_every, len(g)))
+        self._check(_lib.load().swe_run_traces(self.ctx, int(scheme), len(d), d.ctypes.data, len(g), g.ctypes.data,
+                                               int(obs_every), out.ctypes.data))
+        return out
+
 
 class TimeDisc:
     """TimeDisc (include/TimeDisc.h:4-23) over a SpaceDisc."""
@@ -497,6 +517,29 @@ class Batch:
     def set_prim(self, q: int, prim) -> None:
         a = np.ascontiguousarray(prim, dtype=np.float64).reshape(self.sizes[q], 3)
         self._check(_lib.load().swe_batch_set_prim(self.b, int(q), a.ctypes.data))
+
+    def set_prim_device(self, q: int, ptr: int) -> None:
+        """Instance q's state from device memory (C_q x 3 interleaved)."""
+        self._check(_lib.load().swe_batch_set_prim_device(self.b, int(q), ctypes.c_void_p(ptr)))
+
+    def set_bathymetry(self, zs) -> None:
+        """zs: one array of node z per instance (None keeps that instance's)."""
+        keep = [None if z is None else np.ascontiguousarray(z, dtype=np.float64) for z in zs]
+        ptrs = (ctypes.c_void_p * len(keep))(*[None if z is None else z.ctypes.data for z in keep])
+        self._check(_lib.load().swe_batch_set_bathymetry(self.b, ptrs))
+
+    def prime(self) -> None:
+        self._check(_lib.load().swe_batch_prime(self.b))
+
+    def run_traces(self, scheme: int, dts, gauges, obs_every: int) -> np.ndarray:
+        """dts: (n_steps, n_instances); gauges numbered over the concatenated
+        cells.  Returns (n_steps // obs_every, len(gauges))."""
+        d = np.ascontiguousarray(dts, dtype=np.float64)
+        g = np.ascontiguousarray(gauges, dtype=np.int64)
+        out = np.zeros((d.shape[0] // obs_every, len(g)))
+        self._check(_lib.load().swe_batch_run_traces(self.b, int(scheme), d.shape[0], d.ctypes.data, len(g),
+                                                     g.ctypes.data, int(obs_every), out.ctypes.data))
+        return out
 
     def set_time(self, q: int, t: float) -> None:
         self._check(_lib.load().swe_batch_set_time(self.b, int(q), float(t)))
