@@ -298,6 +298,17 @@ swe_status swe_adjoint_forward(swe_ctx* ctx, int32_t scheme, int64_t n_steps, in
 swe_status swe_adjoint_backward(swe_ctx* ctx, const double* trace_grads, double* grad_prim0, double* grad_bathymetry);
 /* The n_steps dts recorded by the last swe_adjoint_forward. */
 swe_status swe_adjoint_dts(swe_ctx* ctx, double* dts_out);
+/* Wetting-front regularisation of the reverse (no reference counterpart).
+ * Where a PartWet2 cell's node maximum comes from a partially-wet neighbour's
+ * PartWet1 level b23 + cbrt(3 h K), that level's slope in w grows like
+ * h^(-2/3) as the depth h -> 0; fed back through PartWet2 over many steps the
+ * exact reverse then grows without bound on beds whose bumps emerge (1e129
+ * after 500 steps of 64 such instances) while the forward stays smooth at
+ * finite perturbations.  Below `depth` the slope is taken at h = depth
+ * (scaled by (h / depth)^(2/3)).  Default 1e-3, the reference's
+ * desingularisation depth (include/Assigners.h:30); 0 gives the exact derivative
+ * of the discrete forward.  Takes effect at the next backward. */
+swe_status swe_adjoint_set_regularisation(swe_ctx* ctx, double depth);
 /* swe_adjoint_forward / swe_adjoint_backward with every array in device memory
  * (gauge_cells stays on the host): traces_out, trace_grads, grad_prim0 (3 x C
  * interleaved, the caller's cell order) and grad_bathymetry (N, the caller's
@@ -382,6 +393,8 @@ swe_status swe_batch_adjoint_forward(swe_batch* b, int32_t scheme, int64_t n_ste
 swe_status swe_batch_adjoint_backward(swe_batch* b, const double* trace_grads, double* grad_prim0,
                                       double* grad_bathymetry);
 swe_status swe_batch_adjoint_dts(swe_batch* b, double* dts_out);
+/* swe_adjoint_set_regularisation for a batch. */
+swe_status swe_batch_adjoint_set_regularisation(swe_batch* b, double depth);
 /* Device-memory forms of the batch adjoint, as for a single context. */
 swe_status swe_batch_adjoint_forward_device(swe_batch* b, int32_t scheme, int64_t n_steps, int64_t checkpoint_every,
                                             int32_t n_gauges, const int64_t* gauge_cells, int64_t obs_every,

@@ -39,7 +39,7 @@ EXPORTS = [
     "swe_batch_set_min_len_to_wavespeed", "swe_adjoint_forward_device", "swe_adjoint_backward_device",
     "swe_run_traces", "swe_set_bathymetry", "swe_prime", "swe_batch_adjoint_forward_device",
     "swe_batch_adjoint_backward_device", "swe_batch_run_traces", "swe_batch_set_bathymetry", "swe_batch_prime",
-    "swe_batch_set_prim_device",
+    "swe_batch_set_prim_device", "swe_adjoint_set_regularisation", "swe_batch_adjoint_set_regularisation",
 ]
 
 
@@ -168,6 +168,8 @@ def load(build_if_needed: bool = True):
         "swe_batch_set_bathymetry": [vp, vp],
         "swe_batch_prime": [vp],
         "swe_batch_set_prim_device": [vp, i32, vp],
+        "swe_adjoint_set_regularisation": [vp, d],
+        "swe_batch_adjoint_set_regularisation": [vp, d],
     }
     for name, args in sig.items():
         f = getattr(L, name)

@@ -44,6 +44,11 @@ class Rollout:
         self.sd._check(_lib.load().swe_adjoint_dts(self.sd.ctx, out.ctypes.data))
         return out
 
+    def set_regularisation(self, depth: float) -> None:
+        """Depth below which the reverse regularises the slope of a partially
+        wet level feeding a node maximum (1e-3 by default; 0 = exact)."""
+        self.sd._check(_lib.load().swe_adjoint_set_regularisation(self.sd.ctx, float(depth)))
+
     def backward(self, trace_grads):
         tg = np.ascontiguousarray(trace_grads, dtype=np.float64)
         gp = np.zeros((self.mesh.num_cells, 3))
@@ -84,6 +89,10 @@ class BatchRollout:
         out = np.zeros((n_steps, len(self.meshes)))
         self.batch._check(_lib.load().swe_batch_adjoint_dts(self.batch.b, out.ctypes.data))
         return out
+
+    def set_regularisation(self, depth: float) -> None:
+        """As Rollout.set_regularisation, for every instance."""
+        self.batch._check(_lib.load().swe_batch_adjoint_set_regularisation(self.batch.b, float(depth)))
 
     def backward(self, trace_grads):
         """trace_grads: one array per instance, shaped like its traces.

@@ -859,6 +859,12 @@ swe_status swe_adjoint_backward_device(swe_ctx* ctx, const double* trace_grads, 
   SWE_GUARD_END(&ctx->err)
 }
 
+swe_status swe_adjoint_set_regularisation(swe_ctx* ctx, double depth) {
+  if (!ctx || !(depth >= 0.) || !std::isfinite(depth)) return SWE_ERR_INVALID_ARGUMENT;
+  ctx->eng.set_adjoint_regularisation(depth);
+  return SWE_OK;
+}
+
 swe_status swe_adjoint_dts(swe_ctx* ctx, double* dts_out) {
   if (!ctx || !dts_out) return SWE_ERR_INVALID_ARGUMENT;
   std::string e = ctx->eng.adjoint_dts(dts_out);
@@ -1135,6 +1141,12 @@ swe_status swe_batch_adjoint_backward_device(swe_batch* b, const double* trace_g
   if (!e.empty()) return fail(&b->err, SWE_ERR_INVALID_ARGUMENT, e);
   return SWE_OK;
   SWE_GUARD_END(&b->err)
+}
+
+swe_status swe_batch_adjoint_set_regularisation(swe_batch* b, double depth) {
+  if (!b || !(depth >= 0.) || !std::isfinite(depth)) return SWE_ERR_INVALID_ARGUMENT;
+  b->eng.set_adjoint_regularisation(depth);
+  return SWE_OK;
 }
 
 swe_status swe_batch_adjoint_dts(swe_batch* b, double* dts_out) {

@@ -19,6 +19,8 @@
 // state is not differentiated.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -684,7 +686,8 @@ __device__ void pw_jacobian(const DevMesh& m, const DevWork& wk, const AdjWork& 
           // desingularisation depth kEta1 the w-slope is taken at h = kEta1
           // (scaled by (h / kEta1)^(2/3)).
           const double hb = W[best] - m.bc[best];
-          if (dltc(hb, kEta1)) J.rc[0] *= dge0(hb) ? cbrt(SWE_DIV(hb * hb, kEta1 * kEta1)) : 0.;
+          const double rd = aw.reg_depth;
+          if (rd > 0. && dltc(hb, rd)) J.rc[0] *= dge0(hb) ? cbrt(SWE_DIV(hb * hb, rd * rd)) : 0.;
         }
       }
     }
@@ -953,6 +956,21 @@ std::string Engine::adjoint_init() {
     for (int64_t i = 0; i < h.C; ++i)
       for (int k = 0; k < 3; ++k) cells[fill[n0 + h.cn[3 * i + k]]++] = (int)(((c0 + i) << 2) | k);
   }
+  // Each node's cells in the caller's cell order: where several cells attain
+  // the node maximum, the reverse routes through the first of them, and that
+  // choice must not depend on the device order the tuner picked.
+  {
+    std::vector<int64_t> caller((size_t)C);
+    for (int q = 0; q < I(); ++q) {
+      const Layout* L = (size_t)q < layouts.size() ? &layouts[q] : nullptr;
+      const bool id = !L || L->identity();
+      for (int64_t j = 0; j < cell_off[q + 1] - cell_off[q]; ++j)
+        caller[cell_off[q] + j] = cell_off[q] + (id ? j : L->cell_from[j]);
+    }
+    for (int64_t n = 0; n < N; ++n)
+      std::sort(cells.begin() + ptr[n], cells.begin() + ptr[n + 1],
+                [&](int a, int b) { return caller[a >> 2] < caller[b >> 2]; });
+  }
   int* d_twin = a->alloc<int>(3 * C);
   int* d_ptr = a->alloc<int>(N + 1);
   int* d_cells = a->alloc<int>(3 * C);
@@ -1131,6 +1149,7 @@ std::string Engine::adjoint_backward(const double* trace_grads_host, double* gra
   }
   AdjointState& a = *adj_;
   AdjWork& w = a.aw;
+  w.reg_depth = adj_reg_depth_;
   const int64_t C = mesh_.C, N = mesh_.N;
   const Scheme sc = a.sc;
   const int ns = sc.n;

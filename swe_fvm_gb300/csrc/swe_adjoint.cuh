@@ -41,6 +41,10 @@ struct AdjWork {
   // neighbour mask q, lp_k = lg0 padj[.][q][k] + lg1 padj[.][q][3 + k]
   // (geometry only; zero for cells next to a wall, which are never fully wet)
   double* padj;
+  // depth below which the w-slope of a PartWet1 level feeding a node maximum
+  // is regularised (the reference's kEta1 = 1e-3 by default; 0: the exact
+  // derivative of the discrete forward)
+  double reg_depth;
 };
 
 }  // namespace swe

@@ -298,6 +298,9 @@ class Engine {
   std::string adjoint_backward(const double* trace_grads_host, double* grad_prim_host, double* grad_z_host,
                                bool device = false);
   std::string adjoint_dts(double* out_host);
+  // Depth below which the reverse regularises the w-slope of a PartWet1 level
+  // that feeds a node maximum (kEta1 by default; 0 = exact derivative).
+  void set_adjoint_regularisation(double depth) { adj_reg_depth_ = depth; }
 
   int C() const { return mesh_.C; }
   int E() const { return mesh_.E; }
@@ -361,6 +364,7 @@ class Engine {
   Scheme custom_{};
   AdjointState* adj_ = nullptr;
   std::vector<std::pair<void*, size_t>> mesh_arrays_;  // device mesh records in upload order
+  double adj_reg_depth_ = kEta1;
 };
 
 // Precompute (swe_precompute.cu): fills the host images of DevMesh arrays for
