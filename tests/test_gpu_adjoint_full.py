@@ -16,8 +16,9 @@ Every perturbed run repeats the taped run's dts (swe_run_traces), so the
 differences see the same discrete map the adjoint differentiates.
 
 Admissibility, stated before any difference is compared:
-  * resolvable: |gradient| >= 1e-3 of the largest over the candidates, so the
-    round-off of the difference (~1e-16 L / eps) stays below ~1e-7 relative;
+  * resolvable: |gradient| >= 1e-3 of the largest over the candidates and the
+    difference of the two losses at least 1e-7 of the loss, so round-off
+    (~1e-16 L / eps) stays below ~1e-7 relative;
   * converged: the central differences at eps and eps / 2 agree to 1e-6
     relative.  A limiter, wet/dry or upwind switch inside the stencil makes
     them disagree (a jump J moves each by ~J / eps), so this certifies that
@@ -25,6 +26,13 @@ Admissibility, stated before any difference is compared:
   * not regularised: the gradient with the wetting-front regularisation of the
     reverse (swe_adjoint_set_regularisation, depth 1e-3, the default) equals
     the exact one (depth 0) to 1e-7 relative.
+  * config 5 only, a condition on the candidates: the bed around the node
+    (its cells' nodes and their neighbours' nodes) has a relief of at least
+    1000 eps.  Where the bed is flatter than the step (parts of these floors
+    are flat to 1e-10), the binary limiter's decisions in the stencil compare
+    offsets smaller than the step, so every perturbed run takes another branch
+    and the differences converge to that branch's slope, not to the
+    derivative at the unperturbed bed.
 On every admissible cell or node the adjoint must agree with the differences
 to 1e-6 relative (the benchmark spec's bound, nothing relaxed); every resolvable and
 converged cell of config 4 must also agree with the exact (unregularised)
@@ -47,6 +55,24 @@ def with_bed(m, z):
     g = m.geometry.copy()
     g[:, 2] = z
     return Mesh(g, m.edge_nodes, m.edge_cells, m.cell_nodes, m.cell_edges, m.cell_neighbours)
+
+
+def bed_relief(m):
+    """max - min of the bed over each node's cells' nodes and their
+    neighbours' nodes."""
+    z = m.geometry[:, 2]
+    cz_max = z[m.cell_nodes].max(axis=1)
+    cz_min = z[m.cell_nodes].min(axis=1)
+    nb = m.cell_neighbours
+    ring_max = np.where(nb >= 0, cz_max[np.maximum(nb, 0)], -np.inf).max(axis=1)
+    ring_min = np.where(nb >= 0, cz_min[np.maximum(nb, 0)], np.inf).min(axis=1)
+    ring_max = np.maximum(ring_max, cz_max)
+    ring_min = np.minimum(ring_min, cz_min)
+    hi = np.full(m.num_nodes, -np.inf)
+    lo = np.full(m.num_nodes, np.inf)
+    np.maximum.at(hi, m.cell_nodes.reshape(-1), np.repeat(ring_max, 3))
+    np.minimum.at(lo, m.cell_nodes.reshape(-1), np.repeat(ring_min, 3))
+    return hi - lo
 
 
 def summary(name, rows):
@@ -79,7 +105,8 @@ def test_config4_initial_surface_gradient_central_differences(gpu):
         sd.SetVolField(p)
         return float(np.sum((sd.run_traces(1, dts, gauges, obs) - target) ** 2))
 
-    assert loss(prim) == float(np.sum((tr - target) ** 2))  # the trace run repeats the taped run
+    L0 = loss(prim)
+    assert L0 == float(np.sum((tr - target) ** 2))  # the trace run repeats the taped run
     wet = np.where(prim[:, 0] - mesh.centroids()[:, 2] > 0.02)[0]
     gmax = np.abs(g_reg[wet]).max()
     rows = []
@@ -92,7 +119,7 @@ def test_config4_initial_surface_gradient_central_differences(gpu):
                 p[c, 0] += s * e
                 v.append(loss(p))
             fd.append((v[0] - v[1]) / (2 * e))
-        resolvable = abs(g_reg[c]) >= 1e-3 * gmax
+        resolvable = abs(g_reg[c]) >= 1e-3 * gmax and abs(2 * EPS * fd[0]) >= 1e-7 * L0
         converged = abs(fd[0] - fd[1]) <= 1e-6 * abs(fd[1])
         unreg = abs(g_reg[c] - g_ex[c]) <= 1e-7 * abs(g_ex[c])
         rows.append({"cell": int(c), "adjoint": float(g_reg[c]), "fd": fd[0],
@@ -145,15 +172,18 @@ def test_config5_bathymetry_gradient_central_differences(gpu):
         out = b.run_traces(1, dts, gcat, obs)
         return np.array([np.sum((out[:, cut[q]:cut[q + 1]] - target[q]) ** 2) for q in range(NI)])
 
-    picks = []
+    L0 = losses(z0)
+    picks, cands = [], []
     for q, m in enumerate(meshes):
         h = prims[q][:, 0] - m.centroids()[:, 2]
         nmin = np.full(m.num_nodes, np.inf)
         np.minimum.at(nmin, m.cell_nodes.reshape(-1), np.repeat(h, 3))
         bnd = np.zeros(m.num_nodes, bool)
         bnd[m.edge_nodes[m.edge_cells[:, 1] < 0].reshape(-1)] = True
-        cand = np.where((nmin > 0.02) & ~bnd)[0]
-        picks.append(np.random.default_rng(500 + q).choice(cand, K, replace=False))
+        relief = bed_relief(m)
+        cand = np.where((nmin > 0.02) & ~bnd & (relief >= 1e3 * EPS))[0]
+        cands.append(cand)
+        picks.append(np.random.default_rng(500 + q).choice(cand, K, replace=False) if len(cand) >= K else None)
     rows = []
     for k in range(K):
         fd = []
@@ -163,15 +193,18 @@ def test_config5_bathymetry_gradient_central_differences(gpu):
                 zs = []
                 for q in range(NI):
                     z = z0[q].copy()
-                    z[picks[q][k]] += s * e
+                    if picks[q] is not None:
+                        z[picks[q][k]] += s * e
                     zs.append(z)
                 v.append(losses(zs))
             fd.append((v[0] - v[1]) / (2 * e))
         for q in range(NI):
+            if picks[q] is None:
+                continue
             nd = picks[q][k]
-            gmax = np.abs(g_reg[q][picks[q]]).max()
+            gmax = np.abs(g_reg[q][cands[q]]).max()
             gr, ge, f0, f1 = g_reg[q][nd], g_ex[q][nd], fd[0][q], fd[1][q]
-            resolvable = bool(abs(gr) >= 1e-3 * gmax and gmax > 0)
+            resolvable = bool(gmax > 0 and abs(gr) >= 1e-3 * gmax and abs(2 * EPS * f0) >= 1e-7 * L0[q])
             converged = bool(abs(f0 - f1) <= 1e-6 * abs(f1))
             unreg = bool(np.isfinite(ge) and abs(gr - ge) <= 1e-7 * abs(ge))
             rows.append({"instance": q, "node": int(nd), "adjoint": float(gr), "fd": float(f0),
