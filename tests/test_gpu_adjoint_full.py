@@ -16,9 +16,10 @@ Every perturbed run repeats the taped run's dts (swe_run_traces), so the
 differences see the same discrete map the adjoint differentiates.
 
 Admissibility, stated before any difference is compared:
-  * resolvable: |gradient| >= 1e-3 of the largest over the candidates (the
-    differences of two losses whose untouched terms cancel exactly keep their
-    round-off well below that) and neither difference exactly zero;
+  * resolvable: |gradient| >= 1e-3 of the largest over the candidates (in
+    config 5 over all instances' candidates: an instance whose gauges barely
+    see its bed has only tiny, cancellation-dominated gradients) and neither
+    difference exactly zero;
   * converged: the central differences at eps and eps / 2 agree to 1e-6
     relative.  A limiter, wet/dry or upwind switch inside the stencil makes
     them disagree (a jump J moves each by ~J / eps), so this certifies that
@@ -182,6 +183,8 @@ def test_config5_bathymetry_gradient_central_differences(gpu):
         cand = np.where((nmin > 0.02) & ~bnd & (relief >= 1e3 * EPS))[0]
         cands.append(cand)
         picks.append(np.random.default_rng(500 + q).choice(cand, K, replace=False) if len(cand) >= K else None)
+    gmax_all = max(float(np.abs(g_reg[q][cands[q]]).max()) for q in range(NI) if len(cands[q]))
+    print(f"\nlargest bathymetry gradient over the candidates: {gmax_all:.3e}")
     rows = []
     for k in range(K):
         fd = []
@@ -200,7 +203,7 @@ def test_config5_bathymetry_gradient_central_differences(gpu):
             if picks[q] is None:
                 continue
             nd = picks[q][k]
-            gmax = np.abs(g_reg[q][cands[q]]).max()
+            gmax = gmax_all
             gr, ge, f0, f1 = g_reg[q][nd], g_ex[q][nd], fd[0][q], fd[1][q]
             resolvable = bool(gmax > 0 and abs(gr) >= 1e-3 * gmax and f0 != 0.0 and f1 != 0.0)
             converged = bool(abs(f0 - f1) <= 1e-6 * abs(f1))
