@@ -20,6 +20,8 @@
 // Link with -lswe_gb300 -lcudart.
 #pragma once
 
+#include <array>
+#include <cmath>
 #include <cstdint>
 #include <stdexcept>
 #include <string>
@@ -99,6 +101,116 @@ struct Domain {
   const Topology& topo;
 };
 
+// VolumeField (include/ValueField.h:31-78 with VolumeIndexer and
+// VolumeDomainWrapper): the 3 x C primitive field (w, u, v per cell) of a
+// domain, with the cell bathymetry b(i) the centroid z (src/ValueField.cpp:
+// 8-10).  prim(i) = {w, u, v} writes through PrimAssigner's rules and
+// cons(i) = {h, hu, hv} through ConsAssigner's (src/Assigners.cpp:8-44),
+// including their dry clamps and thin-film desingularisation; += / -= read the
+// current value back the same way.  Intermediate products are held in
+// volatile doubles so that a compiler contracting multiply-adds cannot change
+// the reference's rounding.
+class VolumeField {
+ public:
+  using Value = std::array<double, 3>;
+
+  explicit VolumeField(const Domain& b, size_t size = 0) : b_(&b), str_(3 * size, 0.) {}
+  size_t Size() const noexcept { return str_.size() / 3; }
+  void Resize(size_t size) { str_.resize(3 * size, 0.); }
+  const double* data() const noexcept { return str_.data(); }
+  double* data() noexcept { return str_.data(); }
+
+  // centroid z: (P(tp) * (1/3, 1/3, 1/3)) row 2 (src/Bathymetry.cpp:24-27)
+  double b(int64_t i) const {
+    const Topology& t = b_->GetTopology();
+    const double k = 1. / 3.;
+    const int64_t* tp = t.cell_nodes + 3 * i;
+    volatile double a0 = b_->geometry[3 * tp[0] + 2] * k, a1 = b_->geometry[3 * tp[1] + 2] * k;
+    volatile double s = a0 + a1;
+    volatile double a2 = b_->geometry[3 * tp[2] + 2] * k;
+    return s + a2;
+  }
+  double w(int64_t i) const { return str_[3 * i]; }
+  double u(int64_t i) const { return str_[3 * i + 1]; }
+  double v(int64_t i) const { return str_[3 * i + 2]; }
+  double h(int64_t i) const { return w(i) - b(i); }
+  double hu(int64_t i) const { return h(i) * u(i); }
+  double hv(int64_t i) const { return h(i) * v(i); }
+  Value prim(int64_t i) const { return {w(i), u(i), v(i)}; }
+  Value cons(int64_t i) const { return {h(i), hu(i), hv(i)}; }
+
+  // PrimAssigner (src/Assigners.cpp:8-20)
+  struct PrimAssigner {
+    VolumeField& f;
+    int64_t i;
+    void operator=(const Value& r) {
+      const double bb = f.b(i);
+      double* c = f.str_.data() + 3 * i;
+      const double hh = r[0] - bb;
+      if (!(hh > 1e-12)) {
+        c[0] = bb; c[1] = 0.; c[2] = 0.;
+        return;
+      }
+      c[0] = r[0]; c[1] = r[1]; c[2] = r[2];
+      if (hh < 1e-3) {
+        volatile double h2 = hh * hh;
+        volatile double num = std::sqrt(2.) * hh;
+        const double sc = num / std::sqrt(h2 + 1e-6);
+        c[1] *= sc;
+        c[2] *= sc;
+      }
+    }
+    Value Get() const { return static_cast<const VolumeField&>(f).prim(i); }
+    void operator+=(const Value& r) { *this = Value{Get()[0] + r[0], Get()[1] + r[1], Get()[2] + r[2]}; }
+    void operator-=(const Value& r) { *this = Value{Get()[0] - r[0], Get()[1] - r[1], Get()[2] - r[2]}; }
+  };
+  // ConsAssigner (src/Assigners.cpp:22-44)
+  struct ConsAssigner {
+    VolumeField& f;
+    int64_t i;
+    void operator=(const Value& r) {
+      const double bb = f.b(i);
+      double* c = f.str_.data() + 3 * i;
+      const double hh = r[0];
+      if (!(hh > 1e-12)) {
+        c[0] = bb; c[1] = 0.; c[2] = 0.;
+        return;
+      }
+      double ih;
+      if (hh < 1e-3) {
+        volatile double h2 = hh * hh;
+        volatile double h3 = h2 * hh;
+        volatile double h4 = h3 * hh;
+        volatile double num = std::sqrt(2.) * hh;
+        ih = num / std::sqrt(h4 + 1e-12);
+      } else {
+        ih = 1. / hh;
+      }
+      c[0] = hh + bb;
+      c[1] = r[1] * ih;
+      c[2] = r[2] * ih;
+    }
+    Value Get() const {  // (w - b, u (w - b), v (w - b))
+      const double hh = f.w(i) - f.b(i);
+      return {hh, f.u(i) * hh, f.v(i) * hh};
+    }
+    void operator+=(const Value& r) {
+      const Value g = Get();
+      *this = Value{g[0] + r[0], g[1] + r[1], g[2] + r[2]};
+    }
+    void operator-=(const Value& r) {
+      const Value g = Get();
+      *this = Value{g[0] - r[0], g[1] - r[1], g[2] - r[2]};
+    }
+  };
+  PrimAssigner prim(int64_t i) { return PrimAssigner{*this, i}; }
+  ConsAssigner cons(int64_t i) { return ConsAssigner{*this, i}; }
+
+ private:
+  const Domain* b_;
+  std::vector<double> str_;
+};
+
 // SpaceDisc (include/SpaceDisc.h:20-48) on the GPU.  `options` carries the
 // settings the reference does not have (CFL coefficient, device order, block
 // size); its defaults are swe_params_default's.
@@ -123,6 +235,11 @@ class SpaceDisc {
     num_nodes_ = t.num_nodes;
     cfl_ = p.cfl;
   }
+  // the reference's construction: SpaceDisc sd{fluxer, domain, v0, cor, tau}
+  // copies v0 (src/MUSCLObject.cpp:8-11)
+  SpaceDisc(const Fluxes::Fluxer& fluxer, const Domain& b, const VolumeField& v0, double cor = 0, double tau = 0,
+            const swe_params* options = nullptr)
+      : SpaceDisc(fluxer, b, v0.data(), cor, tau, options) {}
   SpaceDisc(const SpaceDisc&) = delete;
   SpaceDisc& operator=(const SpaceDisc&) = delete;
   SpaceDisc(SpaceDisc&& o) noexcept { *this = std::move(o); }

@@ -1,12 +1,15 @@
 // Drives the GPU step through the reference's C++ API (swe_fvm_gb300.hpp),
 // written the way the reference's own driver is (examples/Main.cpp): read a
-// mesh and a state, run n SSPRK2 steps with dt = td.CFLdt(), write the state.
+// mesh and a state, fill a VolumeField through its prim(i) assigner, build
+// SpaceDisc sd{fluxer, domain, v0}, run n SSPRK2 steps with dt = td.CFLdt(),
+// write the state.
 //
 // usage: reference_api_main in.bin out.bin
 //   in.bin : int64 N, E, C, n_steps; geometry 3N f64; edge_nodes 2E,
 //            edge_cells 2E, cell_nodes 3C, cell_edges 3C, cell_neighbours 3C
 //            int64; prim 3C f64
-//   out.bin: prim 3C f64, then the sum of the dt used (f64)
+//   out.bin: the assigned initial field 3C f64, the final prim 3C f64, then
+//            the sum of the dt used (f64)
 // Exit codes: 0 ok, 2 DomainError, 3 SolverError, 4 I/O.
 #include <cstdio>
 #include <vector>
@@ -32,10 +35,14 @@ int main(int argc, char** argv) {
   std::fclose(f);
   if (!ok) return 4;
   double t = 0.;
+  std::vector<double> v0_out;
   try {
     Topology topo(N, E, C, en.data(), ec.data(), cn.data(), ce.data(), ct.data());
     Domain dom(geom.data(), topo);
-    SpaceDisc sd(Fluxes::HLLC<Wavespeeds::Einfeldt>, dom, prim.data());
+    VolumeField v0{dom, (size_t)C};
+    for (int64_t i = 0; i < C; ++i) v0.prim(i) = {prim[3 * i], prim[3 * i + 1], prim[3 * i + 2]};
+    v0_out.assign(v0.data(), v0.data() + 3 * C);
+    SpaceDisc sd{Fluxes::HLLC<Wavespeeds::Einfeldt>, dom, v0};
     TimeDisc td(&sd);
     for (int64_t n = 0; n < steps; ++n) {
       const double dt = td.CFLdt();
@@ -52,6 +59,7 @@ int main(int argc, char** argv) {
   }
   std::FILE* o = std::fopen(argv[2], "wb");
   if (!o) return 4;
+  std::fwrite(v0_out.data(), sizeof(double), v0_out.size(), o);
   std::fwrite(prim.data(), sizeof(double), prim.size(), o);
   std::fwrite(&t, sizeof(double), 1, o);
   std::fclose(o);

@@ -44,6 +44,39 @@ def _write(path, m, prim, steps):
         np.ascontiguousarray(prim, dtype=np.float64).tofile(f)
 
 
+def assigned(m, prim):
+    """The field v0.prim(i) = prim[i] leaves: PrimAssigner (src/Assigners.cpp:
+    8-20) with the centroid bathymetry, as the restatement computes it."""
+    import ctypes
+
+    from oracle.oracle import lib as oracle_lib
+
+    L = oracle_lib()
+    bc = m.centroids()[:, 2]
+    out = np.empty_like(prim)
+    tmp_in, tmp_out = np.empty(3), np.empty(3)
+    for i in range(m.num_cells):
+        tmp_in[:] = prim[i]
+        L.oracle_prim_assign(float(bc[i]), tmp_in.ctypes.data_as(ctypes.c_void_p),
+                             tmp_out.ctypes.data_as(ctypes.c_void_p))
+        out[i] = tmp_out
+    return out
+
+
+def test_volume_field_assigners_on_the_host(driver, tmp_path):
+    """The VolumeField written through prim(i) equals the restatement's
+    PrimAssigner cell by cell (thin films, dry cells, velocities), with no GPU:
+    the driver fails only when it reaches the device."""
+    m, prim = scenarios.random_front_case(30, 7)
+    _write(tmp_path / "in.bin", m, prim, 0)
+    r = subprocess.run([driver, str(tmp_path / "in.bin"), str(tmp_path / "out.bin")], capture_output=True, text=True)
+    if r.returncode == 0:
+        raw = np.fromfile(tmp_path / "out.bin", dtype=np.float64)
+        assert np.array_equal(raw[:3 * m.num_cells].reshape(-1, 3), assigned(m, prim))
+    else:
+        pytest.skip("no device here: the field is checked by the GPU test")
+
+
 def test_driver_rejects_a_bad_mesh_with_domain_error(driver, tmp_path):
     m, prim = scenarios.lake_at_rest(4)
     m = m.contiguous()
@@ -62,8 +95,10 @@ def test_driver_equals_the_python_api(gpu, driver, tmp_path):
     r = subprocess.run([driver, str(tmp_path / "in.bin"), str(tmp_path / "out.bin")], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     raw = np.fromfile(tmp_path / "out.bin", dtype=np.float64)
-    got, t = raw[:-1].reshape(-1, 3), raw[-1]
-    sd = SpaceDisc(Fluxes.HLLC(Wavespeeds.Einfeldt), m, prim)
+    C = m.num_cells
+    v0, got, t = raw[:3 * C].reshape(-1, 3), raw[3 * C:-1].reshape(-1, 3), raw[-1]
+    assert np.array_equal(v0, assigned(m, prim))
+    sd = SpaceDisc(Fluxes.HLLC(Wavespeeds.Einfeldt), m, v0)
     td = TimeDisc(sd)
     t_py = 0.0
     for _ in range(n):
