@@ -38,12 +38,14 @@ import numpy as np  # noqa: E402
 # connectivity): per stage read prim 24 + write prim 24 + 6 ids 24 + node xyz
 # 24 x N/C ~ 12 = 84 B; stage 2 re-reads the step's initial state, 24 B.
 BYTES_PER_CELL_STEP = 2 * 84 + 24
-# FP64 instructions issued per SSPRK2 cell-step by the step kernels (ncu
-# smsp__sass_thread_inst_executed_op_fp64_pred_on, per stage: k_flux 73.7 per
-# edge x 1.5 edges per cell + k_update 74 + k_recon1 23.9 + k_drain 7 per cell,
-# plus the few part-wet cells): the bound of the step on GB300, whose FP64 pipe
-# issues one instruction per lane and cycle (DFMA = 2 flops).
-FP64_INST_PER_CELL_STEP = 440
+# FP64 instructions issued per SSPRK2 cell-step by the step kernels: ncu
+# smsp__sass_thread_inst_executed_op_fp64_pred_on summed over the 12 launches
+# of one step of the dam break at lattice 500 (498,002 cells): 2.002e8, i.e.
+# per stage k_flux 62 per edge x 1.5 edges per cell + k_update 75 + k_recon1
+# 24 + k_drain 7 per cell, plus the few part-wet cells.  The bound of the step
+# on GB300, whose FP64 pipe issues one instruction per lane and cycle (DFMA =
+# 2 flops).
+FP64_INST_PER_CELL_STEP = 402
 LATTICE = int(os.environ.get("SWE_BENCH_LATTICE", "708"))
 CFL = 0.15
 
@@ -612,10 +614,12 @@ def run_batch_adjoint(torch, stream):
                        "flux": "HLLC+Einfeldt", "scheme": "SSPRK2", "cfl": 0.4, "mesh_gen_s": round(t_gen, 1)}}
 
 
-# DRAM bytes per SSPRK2 step (dram__bytes_read.sum + dram__bytes_write.sum over
-# the step's 12 kernels, one ncu launch capture of the 1M-cell mesh, lattice
-# 708, the same command line with --profile; tuned order and blocks).
-TRAFFIC_PER_STEP = {708: 1.753e9}
+# DRAM bytes per SSPRK2 step: dram__bytes_read.sum + dram__bytes_write.sum over
+# the step's 12 kernels in one ncu capture of the same command line at lattice
+# 500 (498,002 cells, tuned order and blocks): 844.1 MB, 1695 B per cell,
+# scaled by the cell count to the 999,698-cell mesh (every kernel's bytes grow
+# with its cells or edges).
+TRAFFIC_PER_STEP = {500: 8.441e8, 708: 1.6945e9}
 
 
 def run_reference(args):
