@@ -16,6 +16,7 @@
 from __future__ import annotations
 
 import hashlib
+import re
 import struct
 from typing import NamedTuple
 
@@ -95,13 +96,25 @@ _NODES_PER_TYPE = {1: 2, 2: 3, 3: 4, 4: 4, 5: 8, 6: 6, 7: 5, 8: 3, 9: 6, 10: 9, 
                    27: 5, 28: 6, 29: 20, 30: 35, 31: 56, 92: 64, 93: 125}
 
 
-def _binary_body(data: bytes, name: str, path: str) -> int:
-    """Offset of the first byte after the '$name' line."""
-    key = b"$" + name.encode() + b"\n"
-    at = data.find(key)
-    if at < 0:
+def _binary_body(data: bytes, name: str, path: str, start: int = 0) -> int:
+    """Offset of the first byte after the '$name' line, searched from `start`
+    (the end of the section read before it, so that binary payloads already
+    walked over cannot match) at the start of a line, LF or CRLF."""
+    m = re.compile(rb"(?:\A|(?<=\n))\$" + re.escape(name.encode()) + rb"\r?\n").search(data, start)
+    if m is None:
         raise ValueError(f"{path}: no ${name} section")
-    return at + len(key)
+    return m.end()
+
+
+def _nodes_start(data: bytes, path: str) -> int:
+    """Where to look for $Nodes: after $EndMeshFormat, and after the binary
+    $Entities / $PartitionedEntities sections when present."""
+    pos = _binary_body(data, "EndMeshFormat", path)
+    for sec in ("EndEntities", "EndPartitionedEntities"):
+        m = re.compile(rb"(?:\A|(?<=\n))\$" + sec.encode() + rb"\r?\n").search(data, pos)
+        if m is not None:
+            pos = m.end()
+    return pos
 
 
 def _gmsh_binary(data: bytes, version: str, dsize: int, path: str):
@@ -119,7 +132,7 @@ def _gmsh_binary(data: bytes, version: str, dsize: int, path: str):
         raise ValueError(f"{path}: data size {dsize} is not supported")
     st, i4, f8 = np.dtype(e + st), np.dtype(e + "i4"), np.dtype(e + "f8")
     if version.startswith("4"):
-        pos = _binary_body(data, "Nodes", path)
+        pos = _binary_body(data, "Nodes", path, _nodes_start(data, path))
         n_blocks = int(np.frombuffer(data, st, 4, pos)[0])
         pos += 4 * dsize
         tags, coords = [], []
@@ -132,7 +145,7 @@ def _gmsh_binary(data: bytes, version: str, dsize: int, path: str):
             width = 3 + (dim if parametric else 0)
             coords.append(np.frombuffer(data, f8, count * width, pos).reshape(count, width)[:, :3])
             pos += count * width * 8
-        pos = _binary_body(data, "Elements", path)
+        pos = _binary_body(data, "Elements", path, pos)
         n_blocks = int(np.frombuffer(data, st, 4, pos)[0])
         pos += 4 * dsize
         tris = []
@@ -152,12 +165,12 @@ def _gmsh_binary(data: bytes, version: str, dsize: int, path: str):
         tris = np.concatenate(tris) if tris else np.zeros((0, 3), np.int64)
         return tags, xyz, tris
     # 2.2: the counts are text lines, the records binary
-    pos = _binary_body(data, "Nodes", path)
+    pos = _binary_body(data, "Nodes", path, _nodes_start(data, path))
     end = data.index(b"\n", pos)
     n = int(data[pos:end])
     rec = np.dtype([("tag", i4), ("xyz", f8, (3,))])
     nodes = np.frombuffer(data, rec, n, end + 1)
-    pos = _binary_body(data, "Elements", path)
+    pos = _binary_body(data, "Elements", path, end + 1 + n * rec.itemsize)
     end = data.index(b"\n", pos)
     remaining = int(data[pos:end])
     pos = end + 1

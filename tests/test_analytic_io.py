@@ -114,6 +114,44 @@ def test_read_binary_gmsh41_with_other_blocks(tmp_path, endian):
     _same_mesh(fileio.read_gmsh(str(p)), build_topology(xyz, tri))
 
 
+def _write_gmsh22_binary(path, xyz, tri, nl=b"\n"):
+    # what Gmsh writes for a 2-D model: a point block (type 15) and a line
+    # block (type 1) with 2 tags each before the triangles; `nl` ends the text
+    # lines (LF or CRLF)
+    n, c = len(xyz), len(tri)
+    parts = [b"$MeshFormat" + nl + b"2.2 1 8" + nl, np.array([1], "<i4").tobytes(), nl + b"$EndMeshFormat" + nl]
+    parts += [b"$Nodes" + nl + str(n).encode() + nl]
+    rec = np.zeros(n, np.dtype([("tag", "<i4"), ("xyz", "<f8", (3,))]))
+    rec["tag"] = np.arange(1, n + 1)
+    rec["xyz"] = xyz
+    parts += [rec.tobytes(), nl + b"$EndNodes" + nl + b"$Elements" + nl + str(c + 3).encode() + nl]
+    parts += [np.array([15, 1, 2], "<i4").tobytes(), np.array([1, 7, 7, 1], "<i4").tobytes()]
+    parts += [np.array([1, 2, 2], "<i4").tobytes(), np.array([[2, 3, 3, 1, 2], [3, 3, 3, 2, 3]], "<i4").tobytes()]
+    ids = np.arange(4, c + 4)
+    rows = np.column_stack([ids, np.full(c, 5), np.full(c, 5), np.asarray(tri) + 1]).astype("<i4")
+    parts += [np.array([2, c, 2], "<i4").tobytes(), rows.tobytes(), nl + b"$EndElements" + nl]
+    path.write_bytes(b"".join(parts))
+
+
+@pytest.mark.parametrize("nl", [b"\n", b"\r\n"], ids=["lf", "crlf"])
+def test_read_binary_gmsh22_with_point_and_line_blocks(tmp_path, nl):
+    xyz, tri = _grid(5)
+    p = tmp_path / "b22.msh"
+    _write_gmsh22_binary(p, xyz, tri, nl)
+    _same_mesh(fileio.read_gmsh(str(p)), build_topology(xyz, tri))
+
+
+def test_read_binary_gmsh41_crlf_headers(tmp_path):
+    xyz, tri = _grid(4)
+    p = tmp_path / "b.msh"
+    _write_gmsh41_binary(p, xyz, tri)
+    data = p.read_bytes()
+    for key in (b"$MeshFormat\n", b"$EndMeshFormat\n", b"$Nodes\n", b"$EndNodes\n", b"$Elements\n"):
+        data = data.replace(key, key[:-1] + b"\r\n", 1)
+    p.write_bytes(data)
+    _same_mesh(fileio.read_gmsh(str(p)), build_topology(xyz, tri))
+
+
 def test_read_gmsh_rejects_truncated_binary(tmp_path):
     xyz, tri = _grid(4)
     p = tmp_path / "b.msh"
