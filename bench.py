@@ -242,6 +242,23 @@ def run_gpu(args):
                           "cells": int(sum(e[0].num_cells for e in ens)), "steps": args.steps,
                           "tuning": b.tuning(0)}))
         return
+    if args.thacker_profile:
+        # profiling driver for the small-mesh configuration: the 8192-cell
+        # Thacker bowl (CFL 0.4), warm-up, then exactly K graph-replayed steps
+        # inside the profiled range
+        from swe_fvm_gb300 import scenarios
+
+        tm, tp = scenarios.thacker(64)
+        ts = SpaceDisc(Fluxes.HLLC(Wavespeeds.Einfeldt), tm, tp, cfl=0.4)
+        ts.run_cfl(1, args.warmup)
+        ts.synchronize()
+        torch.cuda.cudart().cudaProfilerStart()
+        ts.run_cfl(1, args.steps)
+        ts.synchronize()
+        torch.cuda.cudart().cudaProfilerStop()
+        print(json.dumps({"thacker_profile": True, "cells": tm.num_cells, "steps": args.steps,
+                          "tuning": ts.tuning()}))
+        return
     mesh, prim, t_gen = workload()
     C = mesh.num_cells
     sd = SpaceDisc(Fluxes.HLLC(Wavespeeds.Einfeldt), mesh, prim, cfl=CFL)
@@ -687,6 +704,8 @@ def main():
     ap.add_argument("--layouts", action="store_true", help="also time every device order of the mesh")
     ap.add_argument("--ensemble-profile", action="store_true",
                     help="only the batched ensemble: warm-up + K steps (for ncu captures)")
+    ap.add_argument("--thacker-profile", action="store_true",
+                    help="only the 8192-cell Thacker bowl: warm-up + K steps (for ncu captures)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
