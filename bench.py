@@ -67,7 +67,7 @@ def workload_config(mesh, world):
 
 
 def run_thacker(torch, stream, steps: int = 1000):
-    """Config: Thacker bowl on [-2,2]^2, 64 x 64 squares x 2 triangles (8192
+    """Workload: Thacker bowl on [-2,2]^2, 64 x 64 squares x 2 triangles (8192
     cells), HLLC + Einfeldt, SSPRK2, CFL 0.4, 1000 steps with dt from the
     device CFL reduction (graph-replayed), beside the single-thread CPU
     restatement on the same run.  The GPU run's states equal the reference's

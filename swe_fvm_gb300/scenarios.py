@@ -81,7 +81,7 @@ class ClassicThacker:
 
 
 def thacker(n: int = 64, quad: int = 100, t: float = 0.0):
-    """Config: [-2,2]^2, n x n squares x 2 triangles (8192 cells at n=64),
+    """Workload: [-2,2]^2, n x n squares x 2 triangles (8192 cells at n=64),
     bed 0.1 (x^2+y^2), Thacker amplitude a = 0.5 (H0 = sqrt(0.3), p0 = q0 = 0)."""
     th = ClassicThacker()
     mesh = structured_square(n, -2.0, 2.0, bathymetry=th.bed)
@@ -100,7 +100,7 @@ def thacker(n: int = 64, quad: int = 100, t: float = 0.0):
 
 # ------------------------------------------------------------------- dam break
 def dam_break(lattice: int = 708, seed_mesh: int = 0, seed_bed: int = 1, n_bumps: int = 8):
-    """Config: Delaunay of a lattice x lattice jittered grid (about 2 lattice^2
+    """Workload: Delaunay of a lattice x lattice jittered grid (about 2 lattice^2
     triangles; 708 -> ~1.0M), Morton order; 8 bumps with heights U[0.05,0.3],
     widths U[0.02,0.1] over a flat floor at 0; w0 = 0.5 for x < 0.3 else 0.2,
     raised to the cell bed where bumps emerge; u = v = 0."""
@@ -174,7 +174,7 @@ def _hump_job(args):
 
 
 def ensemble(n_instances: int = 256, lo: int = 2000, hi: int = 200000, seed0: int = 1000, processes: int = 0):
-    """Config: n_instances seeded instances (instance i uses seed seed0 + i) with
+    """Workload: n_instances seeded instances (instance i uses seed seed0 + i) with
     cell counts log-uniform in [lo, hi].  Generated in `spawn` worker processes
     (safe to call before or after CUDA is initialised in the parent)."""
     import multiprocessing as mp

@@ -84,7 +84,7 @@ def run_fixed(m, prim, flux, ws, scheme, dt, steps, snaps, cor=0.0):
 
 
 def case_thacker64():
-    """Config: Thacker bowl, 64 x 64 x 2 = 8192 cells, HLLC + Einfeldt,
+    """Workload: Thacker bowl, 64 x 64 x 2 = 8192 cells, HLLC + Einfeldt,
     SSPRK2, CFL 0.4, 1000 steps, walls."""
     m, prim = scenarios.thacker(64)
     res = run_cfl(m, prim, "HLLC", "Einfeldt", "SSPRK2", 0.4, 1000, (1, 10, 100, 1000))

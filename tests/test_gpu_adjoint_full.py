@@ -1,12 +1,12 @@
 """The discrete adjoint against central finite differences at the adjoint
 benchmark configurations' full sizes.
 
-Config 4: one 250k-cell instance, 2000 SSPRK2 steps, 64 gauge cells observed
+The 250k-cell run: one 250k-cell instance, 2000 SSPRK2 steps, 64 gauge cells observed
 every 10th step, checkpoint every 50 steps, target traces from a run whose bed
 carries 5 % seeded Gaussian noise; gradient with respect to the initial
 surface, central differences at step 1e-6 on 32 cells drawn at random from the
 wet cells (h > 0.02).
-Config 5: 64 instances of 20k-100k cells, 500 steps, 16 gauges each,
+The 64-instance batch: 64 instances of 20k-100k cells, 500 steps, 16 gauges each,
 checkpoint every 25 steps, the same kind of target; gradient with respect to
 the node bathymetry, central differences at step 1e-6 on 12 nodes per instance
 drawn at random from the interior nodes whose cells are all wet, every
@@ -17,8 +17,8 @@ differences see the same discrete map the adjoint differentiates.
 
 Admissibility, stated before any difference is compared:
   * resolvable: |gradient| >= 1e-3 of the largest over the candidates (in
-    config 5, over the instance's own candidates) and neither difference
-    exactly zero; in config 5 also |gradient| >= 1e-6 per unit of bed height.
+    the batch, over the instance's own candidates) and neither difference
+    exactly zero; in the batch also |gradient| >= 1e-6 per unit of bed height.
     That floor was added after a run in which five nodes far from every gauge,
     with gradients of 7e-9 to 5e-7, disagreed by 1.6e-6 to 3e-3 while their
     differences had converged: such gradients are sums dominated by
@@ -30,7 +30,7 @@ Admissibility, stated before any difference is compared:
   * not regularised: the gradient with the wetting-front regularisation of the
     reverse (swe_adjoint_set_regularisation, depth 1e-3, the default) equals
     the exact one (depth 0) to 1e-7 relative.
-  * config 5 only, a condition on the candidates: the bed around the node
+  * the batch only, a condition on the candidates: the bed around the node
     (its cells' nodes and their neighbours' nodes) has a relief of at least
     1000 eps.  Where the bed is flatter than the step (parts of these floors
     are flat to 1e-10), the binary limiter's decisions in the stencil compare
@@ -38,8 +38,8 @@ Admissibility, stated before any difference is compared:
     and the differences converge to that branch's slope, not to the
     derivative at the unperturbed bed.
 On every admissible cell or node the adjoint must agree with the differences
-to 1e-6 relative (the benchmark spec's bound, nothing relaxed); every resolvable and
-converged cell of config 4 must also agree with the exact (unregularised)
+to 1e-6 relative (the target bound, nothing relaxed); every resolvable and
+converged cell of the 250k-cell run must also agree with the exact (unregularised)
 gradient to 1e-6.  The test prints the whole error distribution.
 """
 import numpy as np
@@ -89,7 +89,7 @@ def summary(name, rows):
         print("   ", {k: (f"{v:.3e}" if isinstance(v, float) else v) for k, v in r.items()})
 
 
-def test_config4_initial_surface_gradient_central_differences(gpu):
+def test_adjoint_250k_initial_surface_gradient_central_differences(gpu):
     steps, obs, ckpt = 2000, 10, 50
     mesh, prim = scenarios.hump_instance(2024, 250000)
     mesh = mesh.contiguous()
@@ -130,7 +130,7 @@ def test_config4_initial_surface_gradient_central_differences(gpu):
                      "rel_exact": abs(g_ex[c] - fd[0]) / max(abs(fd[0]), 1e-300),
                      "resolvable": bool(resolvable), "converged": bool(converged), "unregularised": bool(unreg),
                      "admissible": bool(resolvable and converged and unreg)})
-    summary("config 4 (250k cells, 2000 steps)", rows)
+    summary("250k cells, 2000 steps", rows)
     adm = [r for r in rows if r["admissible"]]
     assert len(adm) >= 8
     assert max(r["rel"] for r in adm) <= BOUND
@@ -138,7 +138,7 @@ def test_config4_initial_surface_gradient_central_differences(gpu):
     assert max(r["rel_exact"] for r in rc) <= BOUND
 
 
-def test_config5_bathymetry_gradient_central_differences(gpu):
+def test_batched_adjoint_64_instances_bathymetry_gradient_central_differences(gpu):
     steps, obs, ckpt, K = 500, 10, 25, 12
     ens = scenarios.adjoint_ensemble(64)
     meshes = [e[0].contiguous() for e in ens]
@@ -214,7 +214,7 @@ def test_config5_bathymetry_gradient_central_differences(gpu):
                          "converged": converged, "unregularised": unreg,
                          "admissible": resolvable and converged and unreg})
     b.set_bathymetry(z0)
-    summary("config 5 (64 instances, 3.85M cells, 500 steps)", rows)
+    summary("64 instances, 3.85M cells, 500 steps", rows)
     adm = [r for r in rows if r["admissible"]]
     assert len(adm) >= 8
     assert max(r["rel"] for r in adm) <= BOUND

@@ -118,7 +118,7 @@ def test_coriolis(gpu):
 
 
 def test_thacker_8192_cells(gpu):
-    """Config: Thacker bowl, 64 x 64 x 2 cells, HLLC + Einfeldt, SSPRK2, CFL
+    """Workload: Thacker bowl, 64 x 64 x 2 cells, HLLC + Einfeldt, SSPRK2, CFL
     0.4, walls: per-step error for the first 10 steps, then 300 more steps
     through the graph-replayed CFL loop against the restatement's loop."""
     m, prim = scenarios.thacker(64, quad=20)

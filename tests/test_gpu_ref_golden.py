@@ -6,7 +6,7 @@ Q20 edits) in jacobi loop order, written by tests/golden/make_ref_fixtures.py.
 Each case is replayed here through the library's public API (SpaceDisc /
 TimeDisc / Solvers, run_cfl) on cuda:0.
 
-Tolerance: the benchmark spec's bounds, per-step relative L2 <= 1e-12 and final-time
+Tolerance: the target bounds, per-step relative L2 <= 1e-12 and final-time
 relative L2 <= 1e-10, are asserted, and so is exact equality (the device path
 computes in the reference's operation order, so every coefficient matches).
 """
@@ -49,7 +49,7 @@ def cfl_replay(m, prim0, d, flux, prefix=""):
 
 
 def test_thacker_8192_cells_1000_steps_equal_reference(gpu):
-    """Config: Thacker bowl 64 x 64 x 2, HLLC + Einfeldt, SSPRK2, CFL 0.4,
+    """Workload: Thacker bowl 64 x 64 x 2, HLLC + Einfeldt, SSPRK2, CFL 0.4,
     1000 steps (graph-replayed, dt from the device CFL reduction)."""
     m, prim0, d = load_reference_vectors("thacker64")
     cfl_replay(m, prim0, d, "HLLC")

@@ -13,7 +13,7 @@ The restatement (oracle/swe_oracle.c) must equal it bit for bit in both
 orders: interface values, source slots, node maxima, fluxes, CFL ratio and
 the state after every step, for every flux plugin and time scheme, on meshes
 with every reconstruction branch (tolerance written: exact equality; the
-spec bound, per-step relative L2 <= 1e-12, is implied).
+target bound, per-step relative L2 <= 1e-12, is implied).
 
 The reference build needs the reference sources and is skipped where they are
 absent; the golden vectors it wrote (tests/golden/ref_*.npz) are checked
@@ -123,7 +123,7 @@ def test_coriolis_equal_reference(order):
 @needs_ref
 @pytest.mark.parametrize("order", ORDERS)
 def test_thacker_8192_cells_equal_reference(order):
-    """Config: Thacker bowl 64 x 64 x 2, HLLC + Einfeldt, SSPRK2, CFL 0.4."""
+    """Workload: Thacker bowl 64 x 64 x 2, HLLC + Einfeldt, SSPRK2, CFL 0.4."""
     m, prim = scenarios.thacker(64, quad=20)
     r = reference.Reference(m, prim, order=ORDERS[order])
     o = Oracle(m, prim, order=ORDERS[order])
@@ -209,6 +209,6 @@ def test_restatement_reproduces_reference_vectors_bowl():
 
 
 def test_restatement_reproduces_reference_vectors_thacker_1000_steps():
-    """Config: Thacker 8192 cells, 1000 CFL-0.4 steps of the reference."""
+    """Workload: Thacker 8192 cells, 1000 CFL-0.4 steps of the reference."""
     m, prim0, d = load_reference_vectors("thacker64")
     _cfl_replay(m, prim0, d, "HLLC")
