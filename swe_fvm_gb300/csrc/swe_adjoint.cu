@@ -36,8 +36,6 @@ namespace {
 
 constexpr double kInfA = __builtin_huge_val();
 
-__device__ __forceinline__ double ldg(const double* p) { return *p; }
-
 // draining time step of the stage (k_drain without the pass reset, so the
 // pass-1 node maxima stay available to the reverse)
 __global__ void __launch_bounds__(256) k_drain_keep(DevMesh m, DevWork wk, const double* __restrict__ W) {
@@ -106,7 +104,7 @@ __global__ void k_set_i64(long long* dst, long long v) {
 // ---------------------------------------------------------------- R1: update
 // nst: the stage's conservative state before ConsAssigner ([3][C], kept by the
 // segment recompute), or null to recompute it from the stage's fluxes.
-__global__ void __launch_bounds__(256) k_adj_update(DevMesh m, DevWork wk, AdjWork aw, const double* Wp,
+__global__ void __launch_bounds__(256, 4) k_adj_update(DevMesh m, DevWork wk, AdjWork aw, const double* Wp,
                                                     const double* Up, const double* Vp, const double* W0,
                                                     const double* U0, const double* V0, const double* nst, Stage st,
                                                     int batched) {
@@ -298,7 +296,7 @@ __global__ void __launch_bounds__(256) k_adj_drain(DevMesh m, DevWork wk, AdjWor
 
 // ---------------------------------------------------------------- R3: flux
 template <int FLUX, int WS>
-__global__ void __launch_bounds__(256) k_adj_flux(DevMesh m, DevWork wk, AdjWork aw, const double* Wp) {
+__global__ void __launch_bounds__(256, 4) k_adj_flux(DevMesh m, DevWork wk, AdjWork aw, const double* Wp) {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= m.E) return;
   const int o = gidx(m, m.eown[e], m.C), nb = m.enb[e];
@@ -843,7 +841,7 @@ __device__ void adj_recon_cell(const DevMesh& m, const DevWork& wk, AdjWork aw, 
 }
 
 template <bool COR0>
-__global__ void __launch_bounds__(256) k_adj_recon(DevMesh m, DevWork wk, AdjWork aw, const double* W,
+__global__ void __launch_bounds__(256, 4) k_adj_recon(DevMesh m, DevWork wk, AdjWork aw, const double* W,
                                                    const double* U, const double* V, int batched) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < m.C) adj_recon_cell<COR0>(m, wk, aw, W, U, V, i, batched);
@@ -1217,7 +1215,6 @@ std::string Engine::adjoint_backward(const double* trace_grads_host, double* gra
       kept[q] = wq;
     }
   }
-  double* lam_cur = w.lam;
   cudaMemsetAsync(w.lam, 0, 3 * C * sizeof(double), stream_);
   cudaMemsetAsync(w.lz, 0, N * sizeof(double), stream_);
   cudaMemsetAsync(w.lscatter, 0, C * sizeof(double), stream_);
@@ -1349,7 +1346,6 @@ std::string Engine::adjoint_backward(const double* trace_grads_host, double* gra
   }
   if (g_rec) cudaGraphExecDestroy(g_rec);
   if (g_rev) cudaGraphExecDestroy(g_rev);
-  (void)lam_cur;
   if (err.empty()) {
     double* d_out = store[0];
     k_interleave<<<gc, b, 0, stream_>>>(lam_step, (int)C, d_out);
@@ -1375,6 +1371,10 @@ std::string Engine::adjoint_backward(const double* trace_grads_host, double* gra
 
 // Threads per block of the reverse kernels: 128 (and 64) measured 3 % faster
 // backward passes than 256 on a 250k-cell mesh (1.83 vs 1.89 s for 2000 steps).
+// k_adj_update, k_adj_flux and k_adj_recon are held at 64 registers
+// (__launch_bounds__(256, 4); 80-97 uncapped): on the 64-instance, 3.85M-cell
+// batch over 500 steps the backward took 5.43 s against 5.49-5.51 s uncapped
+// and 5.43-5.46 s at 72 or 80, with the same gradients.
 constexpr int kReverseBlock = 128;
 
 cudaError_t Engine::adjoint_stage_reverse(const Stage& st, const double* const* in, const double* const* u0,
