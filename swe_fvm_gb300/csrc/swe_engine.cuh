@@ -100,7 +100,9 @@ struct DevMesh {
   const EdgeRec* erec;  // [E] enx, eny, etx, ety, ezm, elmin, packed
   const int4* eidx;     // [E] (eown, enb, eslotl, eslotr), packed
   // nodes
-  const double* nz;  // [N]
+  const double* nz;     // [N]
+  const int* nptr;      // [N+1] the cells around each node (CSR) ...
+  const int* ncell;     // [3C]  ... as (cell << 2) | local node index
   // instances
   const int* inst_cell_begin;  // [I]
   const double* inst_cfl;      // [I]
@@ -371,7 +373,7 @@ class Engine {
 // instance `inst` at offsets (c0, e0, n0) of the concatenated arrays.
 struct HostImage {
   int C, E, N, I;
-  std::vector<int> cnode, cnbr, cedge, cinst, eown, enb, eslotl, eslotr, einst, inst_cell_begin;
+  std::vector<int> cnode, cnbr, cedge, cinst, eown, enb, eslotl, eslotr, einst, inst_cell_begin, nptr, ncell;
   std::vector<unsigned char> cown;
   std::vector<double> bc, fwthr, area, zn, ze, cek, cnxc, cnyc, dry, combo, pw1, enx, eny, etx, ety, ezm, elmin, nz,
       inst_cfl, inst_cor;

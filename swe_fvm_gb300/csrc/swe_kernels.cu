@@ -117,10 +117,41 @@ __device__ __forceinline__ bool at_point_wet(double w0, double off, double z, do
   return false;
 }
 
-__device__ __forceinline__ void node_max(const DevWork& wk, int node, double val, double z) {
-  // max_wp starts at the node z and every AtPoint value is >= z, so values
-  // equal to z cannot raise it.
-  if (dbits(val) != dbits(z)) atomicMax(wk.maxwp + node, order_key(val));
+// Pass-1 AtPoint value of cell c at its local node kn, from what pass 1 left:
+// the class byte (dry / partially wet / fully wet, combination mask, plane
+// kept), the PartWet1 level of a partially-wet cell and the state.
+__device__ __forceinline__ double pass1_value(const DevMesh& m, const DevWork& wk, const double* __restrict__ W,
+                                              int c, int kn) {
+  const int C = m.C;
+  const unsigned cl = wk.cls[c];
+  if ((cl & 3u) == 0u) return m.dry[(size_t)c * kDryStride + kn];
+  const double z = m.zn[kn * C + c];
+  double val;
+  if ((cl & 3u) == 1u) {
+    at_point_wet(wk.pwrec[c], 0., z, &val);  // the PartWet1 level, a flat plane
+  } else {
+    // the combination plane's vertex offset when pass 1 kept the plane, else flat
+    const double off = (cl & 32u) ? m.combo[combo_off(C, c, (int)((cl >> 2) & 7u)) + 8 + kn] : 0.;
+    at_point_wet(W[c], off, z, &val);
+  }
+  return val;
+}
+
+// The node maximum m_max_wp of node nd (src/MUSCLObject.cpp:13-36): the
+// largest pass-1 AtPoint value of the cells around it, starting from the
+// node's bathymetry (every AtPoint value is >= it).  A maximum is exact and
+// order-free, so gathering it where it is needed gives the value the
+// reference's accumulation over its cell loop gives.
+__device__ __forceinline__ unsigned long long node_max_key(const DevMesh& m, const DevWork& wk,
+                                                           const double* __restrict__ W, int nd) {
+  unsigned long long key = order_key(m.nz[nd]);
+  const int q1 = m.nptr[nd + 1];
+  for (int q = m.nptr[nd]; q < q1; ++q) {
+    const int cq = m.ncell[gidx(wk, q, 3 * m.C)];
+    const unsigned long long k = order_key(pass1_value(m, wk, W, gidx(wk, cq >> 2, m.C), cq & 3));
+    key = k > key ? k : key;
+  }
+  return key;
 }
 
 // PartWet1 level (src/MUSCLObject.cpp:86-112)
@@ -169,22 +200,12 @@ __global__ void __launch_bounds__(256, 5) k_recon1(DevMesh m, DevWork wk, const 
       const double* dr = m.dry + (size_t)i * kDryStride;
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
-        node_max(wk, gidx(wk, m.cnode[k * C + i], m.N), dr[k], m.zn[k * C + i]);
         const int slot = k * C + i;
         write_slot<COR0>(wk, slot, m.ze[slot], dr[3 + k], 0., 0., dr[6], dr[7], cor);
       }
     } else if (!dlt(m.fwthr[i], w)) {
-      // partially wet: PartWet1 now (node maxima), PartWet2 in k_recon2
-      const double* p = m.pw1 + (size_t)i * kPw1Stride;
-      const double wr = partwet1_level(p, w, h);
-      wk.pwrec[i] = wr;
-#pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        const double z = m.zn[k * C + i];
-        double val;
-        at_point_wet(wr, 0., z, &val);
-        node_max(wk, gidx(wk, m.cnode[k * C + i], m.N), val, z);
-      }
+      // partially wet: the PartWet1 level now, PartWet2 in k_recon2
+      wk.pwrec[i] = partwet1_level(m.pw1 + (size_t)i * kPw1Stride, w, h);
       part = true;
       cls = 1;
     } else {
@@ -207,7 +228,7 @@ __global__ void __launch_bounds__(256, 5) k_recon1(DevMesh m, DevWork wk, const 
       }
       cls = (unsigned char)(2 | (mask << 2));
       double gx = 0., gy = 0.;
-      double toff[3] = {0., 0., 0.}, noff[3] = {0., 0., 0.};
+      double toff[3] = {0., 0., 0.};
       if (!first_order) {
         const double* rec = m.combo + combo_off(C, i, mask);
         const double g0 = rec[0], g1 = rec[1];
@@ -231,10 +252,7 @@ __global__ void __launch_bounds__(256, 5) k_recon1(DevMesh m, DevWork wk, const 
             gx = g0;
             gy = g1;
 #pragma unroll
-            for (int k = 0; k < 3; ++k) {
-              toff[k] = rec[5 + k];
-              noff[k] = rec[8 + k];
-            }
+            for (int k = 0; k < 3; ++k) toff[k] = rec[5 + k];
           } else {
             gx = 0. * g0;  // diag(TVD) * df keeps the sign of zero
             gy = 0. * g1;
@@ -244,10 +262,6 @@ __global__ void __launch_bounds__(256, 5) k_recon1(DevMesh m, DevWork wk, const 
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
         const int slot = k * C + i;
-        const double zk = m.zn[slot];
-        double val;
-        at_point_wet(w, noff[k], zk, &val);
-        node_max(wk, gidx(wk, m.cnode[slot], m.N), val, zk);
         const double be = m.ze[slot];
         double we;
         if (at_point_wet(w, toff[k], be, &we)) write_slot<COR0>(wk, slot, be, we, u, v, gx, gy, cor);
@@ -268,6 +282,14 @@ __global__ void __launch_bounds__(256, 5) k_recon1(DevMesh m, DevWork wk, const 
   }
 }
 
+// Every node maximum (the reference's m_max_wp after pass 1), for the
+// interface-value entry points that return them; the step itself gathers
+// only the nodes PartWet2 reads (k_recon2).
+__global__ void k_node_max_all(DevMesh m, DevWork wk, const double* __restrict__ W) {
+  const int nd = blockIdx.x * blockDim.x + threadIdx.x;
+  if (nd < m.N) wk.maxwp[nd] = node_max_key(m, wk, W, nd);
+}
+
 // ReconstructPartWetCell2 (src/MUSCLObject.cpp:114-191) over the listed cells.
 template <bool BATCH, bool COR0>
 __global__ void __launch_bounds__(256) k_recon2(DevMesh m, DevWork wk, const double* __restrict__ W,
@@ -285,7 +307,12 @@ __global__ void __launch_bounds__(256) k_recon2(DevMesh m, DevWork wk, const dou
     double gx = 0., gy = 0.;
     bool plane = false;
     if (!(dlt(b13, w) || r.flat)) {
-      const double w23 = order_val(wk.maxwp[gidx(wk, r.lo, m.N)]);
+      // the node maximum of the lowest node, gathered from its cells' pass-1
+      // values; kept in maxwp for the adjoint's reverse of this cell
+      const int lo = gidx(wk, r.lo, m.N);
+      const unsigned long long key = node_max_key(m, wk, W, lo);
+      wk.maxwp[lo] = key;
+      const double w23 = order_val(key);
       const double h23 = w23 - b23;
       const double ratio_b = r.ratio_b;
       const double h_delim1 = 1. / 3. * h23 * ratio_b;
@@ -464,12 +491,10 @@ __global__ void __launch_bounds__(128) k_flux_pw(DevMesh m, DevWork wk, const do
   }
 }
 
-// TimeDisc::ComputeDrainingDt once per cell; also resets the node maxima for
-// the next reconstruction.
+// TimeDisc::ComputeDrainingDt once per cell; also empties the part-wet list
+// for the next reconstruction.
 __global__ void __launch_bounds__(256) k_drain(DevMesh m, DevWork wk, const double* __restrict__ W) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  // the next pass 1 starts from node z and an empty part-wet list
-  if (i < m.N) wk.maxwp[i] = order_key(m.nz[i]);
   if (i == 0) *wk.pwcount = 0;
   if (i >= m.C) return;
   const double h = W[i] - m.bc[i];
@@ -695,6 +720,8 @@ std::string Engine::init(std::vector<HostInstance>&& inst, int flux, int ws, int
   ok = ok && up(img.ety, p_ety) && up(img.ezm, p_ezm) && up(img.elmin, p_elmin) && up(img.nz, p_nz);
   ok = ok && up(img.inst_cell_begin, p_icb) && up(img.inst_cfl, p_cfl) && up(img.inst_cor, p_cor);
   ok = ok && up(img.srec, p_srec) && up(img.cslot, p_cslot) && up(img.erec, p_erec) && up(img.eidx, p_eidx);
+  const int *p_nptr, *p_ncell;
+  ok = ok && up(img.nptr, p_nptr) && up(img.ncell, p_ncell);
   if (!ok) {
     *st = 6;
     return std::string("device allocation or upload failed: ") + cudaGetErrorString(cudaGetLastError());
@@ -706,6 +733,7 @@ std::string Engine::init(std::vector<HostInstance>&& inst, int flux, int ws, int
   M.enx = p_enx; M.eny = p_eny; M.etx = p_etx; M.ety = p_ety; M.ezm = p_ezm; M.elmin = p_elmin;
   M.nz = p_nz; M.inst_cell_begin = p_icb; M.inst_cfl = p_cfl; M.inst_cor = p_cor;
   M.srec = p_srec; M.cslot = p_cslot; M.erec = p_erec; M.eidx = p_eidx;
+  M.nptr = p_nptr; M.ncell = p_ncell;
 
   DevWork& Wk = work_;
   Wk.ew = dalloc<double>(3 * C); Wk.eu = dalloc<double>(3 * C); Wk.ev = dalloc<double>(3 * C);
@@ -805,6 +833,8 @@ void Engine::launch_recon2(const double* W, const double* U, const double* V, cu
 cudaError_t Engine::interface_values(const double* W, const double* U, const double* V, int latch_mode) {
   launch_recon1(W, U, V, latch_mode);
   launch_recon2(W, U, V, stream_);
+  k_node_max_all<<<nblocks(std::max(mesh_.N, 1), 256), 256, 0, stream_>>>(mesh_, work_, W);
+  ++launches_;
   return cudaGetLastError();
 }
 
@@ -892,7 +922,7 @@ cudaError_t Engine::launch_stage(const Stage& st, const double* const* in, const
     if (e != cudaSuccess) return e;
     cudaStreamWaitEvent(stream_, ev_join_, 0);
   }
-  k_drain<<<nblocks(std::max(mesh_.C, mesh_.N), b), b, 0, stream_>>>(mesh_, work_, in[0]);
+  k_drain<<<nblocks(mesh_.C, b), b, 0, stream_>>>(mesh_, work_, in[0]);
   if (ev) cudaEventRecord(ev[4], stream_);
   ++launches_;
   launch_update(st, in, u0, out, nullptr);
@@ -1143,6 +1173,7 @@ std::string Engine::set_bathymetry(const std::vector<const double*>& z) {
   refill(img.ety); refill(img.ezm); refill(img.elmin); refill(img.nz);
   refill(img.inst_cell_begin); refill(img.inst_cfl); refill(img.inst_cor);
   refill(img.srec); refill(img.cslot); refill(img.erec); refill(img.eidx);
+  refill(img.nptr); refill(img.ncell);
   if (!ok || k != mesh_arrays_.size()) return "re-uploading the mesh records failed";
   // the host image must outlive the asynchronous copies
   cudaError_t e = cudaStreamSynchronize(stream_);

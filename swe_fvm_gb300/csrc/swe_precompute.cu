@@ -32,6 +32,7 @@ void HostImage::resize(int C_, int E_, int N_, int I_) {
   eown.assign(E, 0); enb.assign(E, -1); eslotl.assign(E, 0); eslotr.assign(E, -1); einst.assign(E, 0);
   enx.assign(E, 0); eny.assign(E, 0); etx.assign(E, 0); ety.assign(E, 0); ezm.assign(E, 0); elmin.assign(E, 0);
   nz.assign(N, 0);
+  nptr.assign((size_t)N + 1, 0); ncell.assign(3 * (size_t)C, 0);
   inst_cell_begin.assign(I, 0); inst_cfl.assign(I, 0); inst_cor.assign(I, 0);
 }
 
@@ -143,6 +144,17 @@ void precompute_instance(const HostInstance& h, int inst, int64_t c0, int64_t e0
   img.inst_cfl[inst] = h.cfl;
   img.inst_cor[inst] = h.cor;
   for (int64_t n = 0; n < N; ++n) img.nz[n0 + n] = h.geom[3 * n + 2];
+  // the cells around each node, a CSR over this instance's nodes whose
+  // entries start at 3 c0 (each cell has three nodes): PartWet2 gathers its
+  // lowest node's maximum over them (src/MUSCLObject.cpp:138-140)
+  {
+    std::vector<int64_t> at((size_t)N + 1, 0);
+    for (int64_t i = 0; i < 3 * C; ++i) at[h.cn[i] + 1]++;
+    for (int64_t n = 0; n < N; ++n) at[n + 1] += at[n];
+    for (int64_t n = 0; n <= N; ++n) img.nptr[n0 + n] = (int)(3 * c0 + at[n]);
+    for (int64_t i = 0; i < C; ++i)
+      for (int k = 0; k < 3; ++k) img.ncell[3 * c0 + at[h.cn[3 * i + k]]++] = (int)(((c0 + i) << 2) | k);
+  }
 
   auto cell_range = [&](int64_t lo, int64_t hi) {
     for (int64_t i = lo; i < hi; ++i) {
