@@ -40,12 +40,12 @@ import numpy as np  # noqa: E402
 BYTES_PER_CELL_STEP = 2 * 84 + 24
 # FP64 instructions issued per SSPRK2 cell-step by the step kernels: ncu
 # smsp__sass_thread_inst_executed_op_fp64_pred_on summed over the 12 launches
-# of one step of the dam break at lattice 500 (498,002 cells): 2.002e8, i.e.
-# per stage k_flux 62 per edge x 1.5 edges per cell + k_update 75 + k_recon1
-# 24 + k_drain 7 per cell, plus the few part-wet cells.  The bound of the step
-# on GB300, whose FP64 pipe issues one instruction per lane and cycle (DFMA =
-# 2 flops).
-FP64_INST_PER_CELL_STEP = 402
+# of one step of the dam break at lattice 500 (498,002 cells): 1.942e8, i.e.
+# per stage k_flux 62 per edge x 1.5 edges per cell + k_update 73-79 +
+# k_recon1 18 + k_drain 7 per cell, plus the few part-wet cells.  The bound of
+# the step on GB300, whose FP64 pipe issues one instruction per lane and cycle
+# (DFMA = 2 flops).
+FP64_INST_PER_CELL_STEP = 390
 LATTICE = int(os.environ.get("SWE_BENCH_LATTICE", "708"))
 CFL = 0.15
 
@@ -633,10 +633,10 @@ def run_batch_adjoint(torch, stream):
 
 # DRAM bytes per SSPRK2 step: dram__bytes_read.sum + dram__bytes_write.sum over
 # the step's 12 kernels in one ncu capture of the same command line at lattice
-# 500 (498,002 cells, tuned order and blocks): 844.1 MB, 1695 B per cell,
+# 500 (498,002 cells, tuned order and blocks): 802.8 MB, 1612 B per cell,
 # scaled by the cell count to the 999,698-cell mesh (every kernel's bytes grow
 # with its cells or edges).
-TRAFFIC_PER_STEP = {500: 8.441e8, 708: 1.6945e9}
+TRAFFIC_PER_STEP = {500: 8.028e8, 708: 1.6115e9}
 
 
 def run_reference(args):

@@ -309,6 +309,11 @@ swe_status swe_adjoint_dts(swe_ctx* ctx, double* dts_out);
  * desingularisation depth (include/Assigners.h:30); 0 gives the exact derivative
  * of the discrete forward.  Takes effect at the next backward. */
 swe_status swe_adjoint_set_regularisation(swe_ctx* ctx, double depth);
+/* Builds the adjoint's one-time tables and work arrays (the cells around each
+ * node, the twin slots of each edge, the plane-point adjoints of every cell;
+ * built from the bed, so swe_set_bathymetry drops them) ahead of the first
+ * taped run, which otherwise builds them itself.  No reference counterpart. */
+swe_status swe_adjoint_prepare(swe_ctx* ctx);
 /* swe_adjoint_forward / swe_adjoint_backward with every array in device memory
  * (gauge_cells stays on the host): traces_out, trace_grads, grad_prim0 (3 x C
  * interleaved, the caller's cell order) and grad_bathymetry (N, the caller's
@@ -393,6 +398,8 @@ swe_status swe_batch_adjoint_forward(swe_batch* b, int32_t scheme, int64_t n_ste
 swe_status swe_batch_adjoint_backward(swe_batch* b, const double* trace_grads, double* grad_prim0,
                                       double* grad_bathymetry);
 swe_status swe_batch_adjoint_dts(swe_batch* b, double* dts_out);
+/* swe_adjoint_prepare for a batch. */
+swe_status swe_batch_adjoint_prepare(swe_batch* b);
 /* swe_adjoint_set_regularisation for a batch. */
 swe_status swe_batch_adjoint_set_regularisation(swe_batch* b, double depth);
 /* Device-memory forms of the batch adjoint, as for a single context. */

@@ -40,6 +40,7 @@ EXPORTS = [
     "swe_run_traces", "swe_set_bathymetry", "swe_prime", "swe_batch_adjoint_forward_device",
     "swe_batch_adjoint_backward_device", "swe_batch_run_traces", "swe_batch_set_bathymetry", "swe_batch_prime",
     "swe_batch_set_prim_device", "swe_adjoint_set_regularisation", "swe_batch_adjoint_set_regularisation",
+    "swe_adjoint_prepare", "swe_batch_adjoint_prepare",
 ]
 
 
@@ -170,6 +171,8 @@ def load(build_if_needed: bool = True):
         "swe_batch_set_prim_device": [vp, i32, vp],
         "swe_adjoint_set_regularisation": [vp, d],
         "swe_batch_adjoint_set_regularisation": [vp, d],
+        "swe_adjoint_prepare": [vp],
+        "swe_batch_adjoint_prepare": [vp],
     }
     for name, args in sig.items():
         f = getattr(L, name)

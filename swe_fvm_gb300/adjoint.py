@@ -29,6 +29,8 @@ class Rollout:
         self.mesh = mesh.contiguous()
         self.sd = SpaceDisc(fluxer or Fluxes.HLLC(Wavespeeds.Einfeldt), self.mesh, prim0, cor=cor, cfl=cfl,
                             reorder=reorder, block=block)
+        # the adjoint's tables are built with the context, not inside the first taped run
+        self.sd._check(_lib.load().swe_adjoint_prepare(self.sd.ctx))
 
     def forward(self, scheme: int, n_steps: int, checkpoint_every: int, gauges, obs_every: int) -> np.ndarray:
         g = np.ascontiguousarray(gauges, dtype=np.int64)
@@ -69,6 +71,7 @@ class BatchRollout:
         self.cell_off = np.concatenate([[0], np.cumsum([m.num_cells for m in self.meshes])]).astype(np.int64)
         self.node_off = np.concatenate([[0], np.cumsum([m.num_nodes for m in self.meshes])]).astype(np.int64)
         self.gauge_counts = []
+        self.batch._check(_lib.load().swe_batch_adjoint_prepare(self.batch.b))
 
     def forward(self, scheme: int, n_steps: int, checkpoint_every: int, gauges, obs_every: int):
         """gauges: one array of local cell ids per instance.  Returns one

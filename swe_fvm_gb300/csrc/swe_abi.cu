@@ -859,6 +859,16 @@ swe_status swe_adjoint_backward_device(swe_ctx* ctx, const double* trace_grads, 
   SWE_GUARD_END(&ctx->err)
 }
 
+swe_status swe_adjoint_prepare(swe_ctx* ctx) {
+  Trace trace("swe_adjoint_prepare");
+  if (!ctx) return SWE_ERR_INVALID_ARGUMENT;
+  SWE_GUARD_BEGIN
+  std::string e = ctx->eng.adjoint_init();
+  if (!e.empty()) return fail(&ctx->err, SWE_ERR_CUDA, e);
+  return SWE_OK;
+  SWE_GUARD_END(&ctx->err)
+}
+
 swe_status swe_adjoint_set_regularisation(swe_ctx* ctx, double depth) {
   if (!ctx || !(depth >= 0.) || !std::isfinite(depth)) return SWE_ERR_INVALID_ARGUMENT;
   ctx->eng.set_adjoint_regularisation(depth);
@@ -1139,6 +1149,16 @@ swe_status swe_batch_adjoint_backward_device(swe_batch* b, const double* trace_g
   SWE_GUARD_BEGIN
   std::string e = b->eng.adjoint_backward(trace_grads, grad_prim0, grad_bathymetry, true);
   if (!e.empty()) return fail(&b->err, SWE_ERR_INVALID_ARGUMENT, e);
+  return SWE_OK;
+  SWE_GUARD_END(&b->err)
+}
+
+swe_status swe_batch_adjoint_prepare(swe_batch* b) {
+  Trace trace("swe_batch_adjoint_prepare");
+  if (!b) return SWE_ERR_INVALID_ARGUMENT;
+  SWE_GUARD_BEGIN
+  std::string e = b->eng.adjoint_init();
+  if (!e.empty()) return fail(&b->err, SWE_ERR_CUDA, e);
   return SWE_OK;
   SWE_GUARD_END(&b->err)
 }

@@ -279,10 +279,12 @@ class Engine {
   // also keeping the state before ConsAssigner in nst [3][C]
   cudaError_t update_only(const Stage& st, const double* const* in, const double* const* u0, double* const* out,
                           double* nst);
+  // The adjoint's one-time tables and work arrays (node and twin lists, plane
+  // adjoints); a no-op once built.  Returns "" or an error message.
+  std::string adjoint_init();
   // Taped forward run for the adjoint: n_steps CFL steps from the current
   // state, checkpoint every ckpt steps, w at the gauge cells every obs steps
   // into traces_host (n_steps / obs rows).  Returns "" or an error message.
-  std::string adjoint_init();
   // traces_device: traces_host is a device pointer (the traces are copied on
   // the device).
   std::string adjoint_forward(int scheme, int64_t n_steps, int64_t ckpt, const int* gauges, int n_gauges,

@@ -4,9 +4,11 @@
 // A stage (src/Solvers.cpp:5-59) is six kernels over the concatenated cells
 // and edges of every instance:
 //   k_recon1  all cells    SpaceDisc::ComputeInterfaceValues pass 1
-//                          (src/SpaceDisc.cpp:37-45) + node maxima
-//   k_recon2  part-wet     pass 2 (src/SpaceDisc.cpp:47-51), reading the
-//                          pass-1 node maxima only (order-independent)
+//                          (src/SpaceDisc.cpp:37-45), listing the partially
+//                          wet cells
+//   k_recon2  part-wet     pass 2 (src/SpaceDisc.cpp:47-51), gathering the
+//                          node maximum it reads from the pass-1 values of
+//                          the node's cells (order-independent)
 //   k_flux    all edges    SpaceDisc::ComputeFluxes (src/SpaceDisc.cpp:54-74)
 //                          with the flux plugin and the CFL min-reduction,
 //                          except the edges of partially-wet cells
@@ -16,8 +18,8 @@
 //   k_update  all cells    TimeDisc::RHS + ConsAssigner (src/TimeDisc.cpp:3-41,
 //                          src/Assigners.cpp:28-44), an edge-to-cell gather
 // Every read of a stage comes from the start-of-stage state, so results do not
-// depend on the cell order or on scheduling; the only atomics (node maxima,
-// CFL minimum, part-wet list append) are exact max/min/append operations.
+// depend on the cell order or on scheduling; the only atomics (CFL minimum,
+// part-wet list append) are exact min/append operations.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -145,10 +147,23 @@ __device__ __forceinline__ double pass1_value(const DevMesh& m, const DevWork& w
 __device__ __forceinline__ unsigned long long node_max_key(const DevMesh& m, const DevWork& wk,
                                                            const double* __restrict__ W, int nd) {
   unsigned long long key = order_key(m.nz[nd]);
-  const int q1 = m.nptr[nd + 1];
-  for (int q = m.nptr[nd]; q < q1; ++q) {
-    const int cq = m.ncell[gidx(wk, q, 3 * m.C)];
-    const unsigned long long k = order_key(pass1_value(m, wk, W, gidx(wk, cq >> 2, m.C), cq & 3));
+  const int q0 = m.nptr[nd], q1 = m.nptr[nd + 1];
+  // the first 8 cells (a triangulation node has about 6) with their loads
+  // issued together, the rest one by one
+  constexpr int kV = 8;
+  int cq[kV];
+#pragma unroll
+  for (int j = 0; j < kV; ++j) cq[j] = q0 + j < q1 ? m.ncell[gidx(wk, q0 + j, 3 * m.C)] : -1;
+#pragma unroll
+  for (int j = 0; j < kV; ++j) {
+    if (cq[j] >= 0) {
+      const unsigned long long k = order_key(pass1_value(m, wk, W, gidx(wk, cq[j] >> 2, m.C), cq[j] & 3));
+      key = k > key ? k : key;
+    }
+  }
+  for (int q = q0 + kV; q < q1; ++q) {
+    const int c = m.ncell[gidx(wk, q, 3 * m.C)];
+    const unsigned long long k = order_key(pass1_value(m, wk, W, gidx(wk, c >> 2, m.C), c & 3));
     key = k > key ? k : key;
   }
   return key;
